@@ -1,0 +1,262 @@
+/*
+ * tfg.h -- C ABI of the GB300 engine for Tissue Forge's per-step particle path.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and returns
+ * an int status (TFG_OK == 0, negative TFG_E_* on failure).  The message of the
+ * last failure on an engine is available from tfg_last_error().
+ *
+ * The data model mirrors the reference's mdcore engine:
+ *   - an engine owns a periodic space split into cells (source/mdcore/include/tfSpace.h:127-243),
+ *   - particles live in cells with cell-relative coordinates (tfParticle.h:101-287),
+ *   - interactions come from tabulated Potential objects (tfPotential.h:213-253), DPD
+ *     potentials (tfDPDPotential.h), Fluxes (tfFlux.h:53-62), Bonds (tfBond.h) and Angles
+ *     (tfAngle.h),
+ *   - one step runs force_prep -> force -> advance (tfEngine.cpp:1378-1557,
+ *     tf_engine_advance.cpp:309-480).
+ *
+ * Threading: one host thread per engine handle; all device work of a handle is ordered
+ * on that handle's CUDA stream (tfg_engine_set_stream may supply the caller's stream).
+ */
+#ifndef TFG_H
+#define TFG_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define TFG_API __attribute__((visibility("default")))
+#else
+#define TFG_API
+#endif
+
+/* ---- status codes (the reference returns HRESULT S_OK / E_FAIL, include/tf_port.h:255-260) ---- */
+#define TFG_OK            0
+#define TFG_E_INVAL      -1   /* bad argument or unsupported configuration */
+#define TFG_E_OOM        -2   /* device or host allocation failed / arena budget exceeded */
+#define TFG_E_CUDA       -3   /* a CUDA runtime call failed */
+#define TFG_E_TOOFAST    -4   /* a particle moved more than one cell in a step (tf_engine_advance.cpp:204-206) */
+#define TFG_E_TIMEOUT    -5   /* a bounded device wait ran out */
+#define TFG_E_OVERFLOW   -6   /* a per-cell or per-tile capacity was exceeded */
+#define TFG_E_RANGE      -7   /* a particle lies outside the space (tfSpace.cpp:444-448) */
+#define TFG_E_STATE      -8   /* call made in the wrong state (e.g. step before load) */
+#define TFG_E_NAN        -9   /* a non-finite position or force was produced */
+#define TFG_E_NODEVICE  -10   /* no CUDA device is available */
+
+/* ---- potential kinds and flags: values of the reference enums (tfPotential.h:56-122) ---- */
+#define TFG_POTENTIAL_KIND_POTENTIAL 0u   /* tabulated piecewise quintic */
+#define TFG_POTENTIAL_KIND_DPD       1u   /* dissipative particle dynamics */
+
+#define TFG_POTENTIAL_R2        (1u << 4)
+#define TFG_POTENTIAL_ANGLE     (1u << 6)
+#define TFG_POTENTIAL_HARMONIC  (1u << 7)
+#define TFG_POTENTIAL_SCALED    (1u << 11)
+#define TFG_POTENTIAL_SHIFTED   (1u << 12)
+#define TFG_POTENTIAL_LJ126     (1u << 0)
+
+/* Number of float coefficients per interval (potential_chunk, tfPotential.h:40). */
+#define TFG_POTENTIAL_CHUNK 8
+/* Largest interval count a table may have (potential_ivalsmax, tfPotential.h:45). */
+#define TFG_POTENTIAL_IVALSMAX 3048
+
+/*
+ * A potential as the reference stores it (struct Potential, tfPotential.h:213-253):
+ * table coefficients c[(n+1)*8] plus the index transform alpha[0..2].  For DPD the
+ * table is empty (c == NULL) and dpd_alpha/gamma/sigma hold DPDPotential's fields
+ * (tfDPDPotential.cpp:32-43); a = sqrt(FLT_EPSILON), b = cutoff.
+ */
+typedef struct tfg_potential {
+    uint32_t kind;
+    uint32_t flags;
+    float alpha[4];
+    float r0_plusone;
+    float a, b;
+    int32_t n;
+    const float *c;          /* (n+1)*TFG_POTENTIAL_CHUNK floats; owned by the creator */
+    float dpd_alpha, dpd_gamma, dpd_sigma;
+} tfg_potential;
+
+/* ---- table construction: the reference's Potential factories (tfPotential.cpp) ----
+ * Each builds the table on the host exactly as potential_init() does
+ * (tfPotential.cpp:1396-1634) and returns a library-owned object; free it with
+ * tfg_potential_free().  Arguments and defaults follow the factories cited. */
+
+/* Potential::morse (tfPotential.cpp:3068-3084 -> potential_create_morse :2249-2283) */
+TFG_API int tfg_potential_morse(float d, float a, float r0, float min, float max, float tol,
+                                int shifted, tfg_potential **out);
+/* Potential::lennard_jones_12_6 (tfPotential.cpp:2741-2751 -> potential_create_LJ126 :1087-1109);
+ * tol <= 0 selects the reference default 0.001*(max-min). */
+TFG_API int tfg_potential_lennard_jones_12_6(float min, float max, float A, float B, float tol,
+                                             tfg_potential **out);
+/* Potential::harmonic (tfPotential.cpp:2961-2975 -> potential_create_harmonic :374-401);
+ * min < 0 / max < 0 / tol <= 0 select the reference defaults r0-r0, r0+r0, 0.01*(max-min). */
+TFG_API int tfg_potential_harmonic(float k, float r0, float min, float max, float tol,
+                                   tfg_potential **out);
+/* Potential::harmonic_angle (tfPotential.cpp:2991-3003 -> potential_create_harmonic_angle :594-626);
+ * min < 0 / max < 0 / tol <= 0 select the defaults 0, pi, 0.005*(max-min). */
+TFG_API int tfg_potential_harmonic_angle(float k, float theta0, float min, float max, float tol,
+                                         tfg_potential **out);
+/* Potential::dpd (tfPotential.cpp:3128-3142 -> DPDPotential ctor tfDPDPotential.cpp:32-43) */
+TFG_API int tfg_potential_dpd(float alpha, float gamma, float sigma, float cutoff, int shifted,
+                              tfg_potential **out);
+TFG_API void tfg_potential_free(tfg_potential *p);
+/* Evaluate a table the way potential_eval_ex does (tf_potential_eval.h:104-146), for
+ * r2 = squared distance and radii ri, rj.  Returns 1 when in range, else 0. */
+TFG_API int tfg_potential_eval(const tfg_potential *p, float ri, float rj, float r2,
+                               float *e, float *f);
+
+/* ---- fluxes (struct Flux, tfFlux.h:53-62; Fluxes::create tfFlux.cpp:56-112) ---- */
+#define TFG_FLUX_FICK     0
+#define TFG_FLUX_SECRETE  1
+#define TFG_FLUX_UPTAKE   2
+#define TFG_MAX_FLUX_PER_PAIR 8   /* TF_SIMD_SIZE (CMakeLists.txt:82) */
+
+typedef struct tfg_flux {
+    int32_t kind;          /* TFG_FLUX_* */
+    int32_t type_a, type_b;  /* orientation (type_ids[i].a/.b) */
+    int32_t index_a, index_b;/* species index in a's and b's state vector */
+    float coef, decay, target, cutoff;  /* cutoff <= 0 -> engine cutoff (tfFlux.cpp:95-96) */
+} tfg_flux;
+
+/* ---- particle types (engine::types[], tfParticle.h ParticleType) ---- */
+#define TFG_NEWTONIAN   0   /* PARTICLE_NEWTONIAN  (tfParticle.h:62-65) */
+#define TFG_OVERDAMPED  1   /* PARTICLE_OVERDAMPED */
+
+/* particle flags (ParticleFlags, tfParticle.h:68-78) */
+#define TFG_PARTICLE_FROZEN_X (1u << 3)
+#define TFG_PARTICLE_FROZEN_Y (1u << 4)
+#define TFG_PARTICLE_FROZEN_Z (1u << 5)
+
+/* ---- engine ---- */
+typedef struct tfg_engine tfg_engine;
+
+/* Engine description: UniverseConfig / engine_init arguments (tfUniverse.cpp:102-120,
+ * tfEngine.cpp:1702-1874, tfSpace.cpp:715-770).  cells[k] is the cell count per axis
+ * (space_init computes cdim = floor(dim/L)); every cell edge must be >= cutoff (a 27-cell
+ * stencil, span 1) and every cells[k] >= 3. */
+typedef struct tfg_engine_desc {
+    float origin[3];
+    float dim[3];
+    int32_t cells[3];
+    float cutoff;
+    float dt;
+    int32_t max_type;                 /* number of particle types */
+    int32_t nr_species;               /* species per particle state vector (0 = none) */
+    float particle_max_dist_fraction; /* reference default 0.05 (tfEngine.cpp:1865) */
+    uint64_t seed;                    /* Philox key for the random terms */
+    int32_t capacity;                 /* maximum particles (0 -> sized at first load) */
+    int32_t max_bonds;                /* capacity for bonds (0 -> sized at load) */
+    int32_t max_angles;               /* capacity for angles (0 -> sized at load) */
+    int32_t device;                   /* CUDA device ordinal */
+    uint32_t flags;                   /* TFG_ENGINE_* */
+} tfg_engine_desc;
+
+/* Engine flags.
+ * TFG_ENGINE_DPD_REFERENCE_RANDOM: reproduce the reference's DPD "random" term, which
+ *   is the constant sigma*omega/sqrt(dt) (tf_dpd_eval.h:64; the Gaussian argument is never
+ *   used).  Without it the term is sigma*omega*xi/sqrt(dt) with xi ~ N(0,1) drawn from a
+ *   Philox4x32-10 stream keyed on (seed, step, min id, max id).
+ * TFG_ENGINE_NO_DENSITY: skip the number-density side output f[3]
+ *   (tf_runner_dopair.cpp:175-177). */
+#define TFG_ENGINE_DPD_REFERENCE_RANDOM (1u << 0)
+#define TFG_ENGINE_NO_DENSITY           (1u << 1)
+
+/* FP64 per-step totals (the reference sums in FPTYPE: tf_engine_advance.cpp:459-470,
+ * tfEngine.cpp:1893+). */
+typedef struct tfg_reductions {
+    double epot;             /* nonbond + bond + angle */
+    double epot_nonbond;
+    double epot_bond;
+    double epot_angle;
+    double kinetic;          /* 0.5 * m * |v|^2 summed, at force_prep (before the step) */
+    double virial;           /* sum over pairs and bonds of f_ij . r_ij */
+    double computed_volume;  /* sum of 1/number_density (tf_engine_advance.cpp:188,239) */
+    double species_total[8]; /* per-species sum of state values after the step */
+    int64_t steps;           /* engine time (number of steps taken) */
+    int64_t migrations;      /* particles that changed cell in the last step */
+} tfg_reductions;
+
+TFG_API int tfg_engine_create(const tfg_engine_desc *desc, tfg_engine **out);
+TFG_API int tfg_engine_destroy(tfg_engine *eng);
+TFG_API const char *tfg_last_error(const tfg_engine *eng);
+/* Use the caller's CUDA stream (a cudaStream_t passed as void*); NULL restores the engine's own. */
+TFG_API int tfg_engine_set_stream(tfg_engine *eng, void *stream);
+
+/* ParticleType dynamics and mass (mass only enters the kinetic energy, tfEngine.cpp:1912). */
+TFG_API int tfg_set_type(tfg_engine *eng, int type, int dynamics, float mass);
+/* engine_addpot (tfEngine.cpp:1054-1077): stores p for (ti,tj) and (tj,ti).  The table is copied. */
+TFG_API int tfg_set_potential(tfg_engine *eng, int ti, int tj, const tfg_potential *p);
+/* engine_addfluxes (tfEngine.cpp:1079-1099) + Fluxes::addFlux (tfFlux.cpp:204-246): appends one
+ * flux to the (ti,tj) Fluxes (at most TFG_MAX_FLUX_PER_PAIR). */
+TFG_API int tfg_add_flux(tfg_engine *eng, int ti, int tj, const tfg_flux *flux);
+/* Species flags per species index: bit0 = SPECIES_KONSTANT (tfFlux.cpp:177-179). */
+TFG_API int tfg_set_species_flags(tfg_engine *eng, int nr, const uint32_t *flags);
+/* Gaussian single-body force per type (Force::random, tfForce.cpp:111-245): redraw
+ * when (time + id) % duration_steps == 0; std <= 0 disables. */
+TFG_API int tfg_set_random_force(tfg_engine *eng, int type, float mean, float std, int duration_steps);
+
+/* Load n particles with GLOBAL positions (space_addpart -> space_setpartp,
+ * tfSpace.cpp:432-475).  Particle i gets id i.  Any pointer except x may be NULL:
+ * v -> 0, type -> 0, radius -> 1, imass -> 1, flags -> 0, species -> 0, force_i -> 0. */
+TFG_API int tfg_load_particles(tfg_engine *eng, int n, const float *x, const float *v,
+                               const int32_t *type, const float *radius, const float *imass,
+                               const uint32_t *flags, const float *species, const float *force_i);
+/* Load n particles already binned: cell index (space_cellid order, x-major) and
+ * cell-relative position, as the reference stores them (tfSpace_cell.h:103-156).
+ * Used for bit-exact state transfer from a reference engine. */
+TFG_API int tfg_load_particles_binned(tfg_engine *eng, int n, const int32_t *cell, const float *xrel,
+                                      const float *v, const int32_t *type, const float *radius,
+                                      const float *imass, const uint32_t *flags,
+                                      const float *species, const float *force_i);
+/* Bond potentials live in numbered slots; bonds and angles name a slot. */
+TFG_API int tfg_set_bonded_potential(tfg_engine *eng, int slot, const tfg_potential *p);
+/* Bond::create (tfBond.cpp:638) for n bonds (i[k], j[k]) using potential slot[k] (NULL -> 0). */
+TFG_API int tfg_load_bonds(tfg_engine *eng, int n, const int32_t *i, const int32_t *j, const int32_t *slot);
+/* Angle::create for n angles (i,j,k) with j the vertex (tfAngle.cpp:90-382). */
+TFG_API int tfg_load_angles(tfg_engine *eng, int n, const int32_t *i, const int32_t *j,
+                            const int32_t *k, const int32_t *slot);
+
+/* Run nsteps full engine steps on the device (engine_step, tfEngine.cpp:1378-1429):
+ * re-bin -> nonbond pair pass -> bonds -> angles -> forward-Euler advance -> flux
+ * integration -> FP64 reductions.  Asynchronous on the engine's stream unless an error
+ * needs reporting; tfg_sync() waits and returns any device-side error. */
+TFG_API int tfg_step(tfg_engine *eng, int nsteps);
+/* Forces only: the reference's engine_nonbond_cuda (tfRunner_cuda.cu:2940-3354) + bonded
+ * forces, without the advance.  Leaves f, number density and flux increments readable. */
+TFG_API int tfg_force_only(tfg_engine *eng, int with_bonded);
+TFG_API int tfg_sync(tfg_engine *eng);
+/* Pair-set signature of the current binned state, per particle id: the number of
+ * partners with r2 <= cutoff^2 and the wrap-around sum of a 32-bit mix of their ids.
+ * It runs the pair pass's own stencil walk and pair decision (no forces).  Call it after
+ * tfg_force_only to describe the pair set that pass used.  Verification hook; the
+ * reference has no counterpart. */
+TFG_API int tfg_pair_signature(tfg_engine *eng, int32_t *count, uint32_t *hash);
+
+TFG_API int tfg_get_count(const tfg_engine *eng, int *n);
+/* Download per-particle state in id order.  Any pointer may be NULL.
+ *   x: global position (cell origin + relative), xrel: cell-relative, cell: cell index,
+ *   f: force (f[0..2]), density: number density f[3], q: flux increments (n*nr_species),
+ *   species: state values (n*nr_species). */
+TFG_API int tfg_download(tfg_engine *eng, float *x, float *xrel, int32_t *cell, float *v, float *f,
+                         float *density, float *species, float *q);
+TFG_API int tfg_get_reductions(tfg_engine *eng, tfg_reductions *out);
+
+/* Per-step timing of the device phases of the last tfg_step call, in milliseconds
+ * (CUDA events on the engine stream): [0] bin, [1] pair, [2] bonded, [3] advance. */
+TFG_API int tfg_get_phase_ms(tfg_engine *eng, float ms[4]);
+
+/* Measured FP32 FMA throughput of `device` in TFLOP/s (2 flops per FMA), from a
+ * register-only kernel with eight independent FMA chains per thread.  Measurement
+ * helper for roofline reporting; the reference has no counterpart. */
+TFG_API int tfg_probe_fp32_tflops(int device, double *tflops);
+
+/* Library build information: returns a static string. */
+TFG_API const char *tfg_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TFG_H */

@@ -1,0 +1,262 @@
+"""Python wrapper of the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: the oracle is the checker of the GPU engine.  Only the
+tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.  It
+restates the reference's mdcore CPU engine; see tfg_oracle.cpp for the file:line
+map.  Parity is unpinned by the reference (which cannot be built here and holds no
+golden vectors for this path); it is pinned by known-answer tests and by the
+fixtures under tests/golden/.
+"""
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "tissue-forge_gb300"))
+from tfg import abi  # noqa: E402  (struct layouts of include/tfg.h)
+
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+MODE_FP64 = 1
+MODE_BRUTE = 2
+MODE_REF_DPD_RANDOM = 4
+MODE_NO_DENSITY = 8
+
+
+def build(force=False):
+    """Compile the oracle with the reference's FP rules (no FMA contraction)."""
+    src = os.path.join(HERE, "tfg_oracle.cpp")
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+        return LIB_PATH
+    cmd = ["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+           "-I" + os.path.join(ROOT, "include"), "-o", LIB_PATH, src, "-lpthread"]
+    subprocess.check_call(cmd)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        L = _lib
+        E = C.c_void_p
+        L.tfo_create.argtypes = [C.POINTER(abi.EngineDesc), C.c_int, C.c_int, C.POINTER(E)]
+        L.tfo_destroy.argtypes = [E]
+        L.tfo_destroy.restype = None
+        L.tfo_set_type.argtypes = [E, C.c_int, C.c_int, C.c_float]
+        L.tfo_set_potential.argtypes = [E, C.c_int, C.c_int, abi.P_POT]
+        L.tfo_add_flux.argtypes = [E, C.c_int, C.c_int, C.POINTER(abi.Flux)]
+        L.tfo_set_species_flags.argtypes = [E, C.c_int, abi.U_P]
+        L.tfo_set_random_force.argtypes = [E, C.c_int, C.c_float, C.c_float, C.c_int]
+        L.tfo_load_particles.argtypes = [E, C.c_int, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P,
+                                         abi.U_P, abi.F_P, abi.F_P]
+        L.tfo_load_particles_binned.argtypes = [E, C.c_int, abi.I_P, abi.F_P, abi.F_P, abi.I_P, abi.F_P,
+                                                abi.F_P, abi.U_P, abi.F_P, abi.F_P]
+        L.tfo_bin.argtypes = [E, C.c_int, abi.F_P, abi.I_P, abi.F_P]
+        L.tfo_set_bonded_potential.argtypes = [E, C.c_int, abi.P_POT]
+        L.tfo_load_bonds.argtypes = [E, C.c_int, abi.I_P, abi.I_P, abi.I_P]
+        L.tfo_load_angles.argtypes = [E, C.c_int, abi.I_P, abi.I_P, abi.I_P, abi.I_P]
+        L.tfo_step.argtypes = [E, C.c_int]
+        L.tfo_force_only.argtypes = [E, C.c_int]
+        L.tfo_download.argtypes = [E, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P]
+        L.tfo_download_forces_f64.argtypes = [E, C.POINTER(C.c_double)]
+        L.tfo_download_fmag.argtypes = [E, C.POINTER(C.c_double)]
+        L.tfo_get_reductions.argtypes = [E, C.POINTER(abi.Reductions)]
+        L.tfo_get_stats.argtypes = [E, C.POINTER(C.c_int64)]
+        L.tfo_signature.argtypes = [E, abi.I_P, abi.U_P]
+        L.tfo_record_pairs.argtypes = [E, C.c_int]
+        L.tfo_get_pairs.argtypes = [E, abi.I_P, C.c_int64]
+        L.tfo_get_pairs.restype = C.c_int64
+        L.tfo_philox_probe.argtypes = [C.c_uint32] * 6 + [C.POINTER(C.c_uint32)]
+        L.tfo_philox_probe.restype = C.c_uint32
+    return _lib
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(abi.F_P)
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(abi.I_P)
+
+
+def _up(a):
+    return None if a is None else a.ctypes.data_as(abi.U_P)
+
+
+def _chk(rc, what):
+    if rc != 0:
+        raise RuntimeError("oracle %s failed: %s" % (what, abi.STATUS_NAMES.get(rc, rc)))
+
+
+class OracleEngine:
+    """CPU restatement of one Tissue Forge engine (space + potentials + fluxes + bonds)."""
+
+    def __init__(self, desc, mode=0, threads=1):
+        self.L = lib()
+        self.h = C.c_void_p()
+        self.desc = desc
+        self.nspec = desc.nr_species
+        _chk(self.L.tfo_create(C.byref(desc), mode, threads, C.byref(self.h)), "create")
+        self.n = 0
+
+    def close(self):
+        if self.h:
+            self.L.tfo_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_type(self, t, dynamics, mass=1.0):
+        _chk(self.L.tfo_set_type(self.h, t, dynamics, mass), "set_type")
+
+    def set_potential(self, ti, tj, pot):
+        _chk(self.L.tfo_set_potential(self.h, ti, tj, pot), "set_potential")
+
+    def add_flux(self, ti, tj, flux):
+        _chk(self.L.tfo_add_flux(self.h, ti, tj, C.byref(flux)), "add_flux")
+
+    def set_species_flags(self, flags):
+        a = np.ascontiguousarray(flags, np.uint32)
+        _chk(self.L.tfo_set_species_flags(self.h, len(a), _up(a)), "set_species_flags")
+
+    def set_random_force(self, t, mean, std, duration_steps):
+        _chk(self.L.tfo_set_random_force(self.h, t, mean, std, duration_steps), "set_random_force")
+
+    def set_bonded_potential(self, slot, pot):
+        _chk(self.L.tfo_set_bonded_potential(self.h, slot, pot), "set_bonded_potential")
+
+    def load(self, x, v=None, type=None, radius=None, imass=None, flags=None, species=None, force_i=None):
+        x = np.ascontiguousarray(x, np.float32)
+        self.n = x.shape[0]
+        conv = lambda a, dt: None if a is None else np.ascontiguousarray(a, dt)
+        v, radius, imass, species, force_i = (conv(a, np.float32) for a in (v, radius, imass, species, force_i))
+        type = conv(type, np.int32)
+        flags = conv(flags, np.uint32)
+        _chk(self.L.tfo_load_particles(self.h, self.n, _fp(x), _fp(v), _ip(type), _fp(radius), _fp(imass),
+                                       _up(flags), _fp(species), _fp(force_i)), "load")
+
+    def load_binned(self, cell, xrel, v=None, type=None, radius=None, imass=None, flags=None, species=None,
+                    force_i=None):
+        cell = np.ascontiguousarray(cell, np.int32)
+        xrel = np.ascontiguousarray(xrel, np.float32)
+        self.n = cell.shape[0]
+        conv = lambda a, dt: None if a is None else np.ascontiguousarray(a, dt)
+        v, radius, imass, species, force_i = (conv(a, np.float32) for a in (v, radius, imass, species, force_i))
+        type = conv(type, np.int32)
+        flags = conv(flags, np.uint32)
+        _chk(self.L.tfo_load_particles_binned(self.h, self.n, _ip(cell), _fp(xrel), _fp(v), _ip(type),
+                                              _fp(radius), _fp(imass), _up(flags), _fp(species), _fp(force_i)),
+             "load_binned")
+
+    def bin(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        n = x.shape[0]
+        cell = np.zeros(n, np.int32)
+        xrel = np.zeros((n, 3), np.float32)
+        _chk(self.L.tfo_bin(self.h, n, _fp(x), _ip(cell), _fp(xrel)), "bin")
+        return cell, xrel
+
+    def load_bonds(self, i, j, slot=None):
+        i = np.ascontiguousarray(i, np.int32)
+        j = np.ascontiguousarray(j, np.int32)
+        slot = None if slot is None else np.ascontiguousarray(slot, np.int32)
+        _chk(self.L.tfo_load_bonds(self.h, len(i), _ip(i), _ip(j), _ip(slot)), "load_bonds")
+
+    def load_angles(self, i, j, k, slot=None):
+        i, j, k = (np.ascontiguousarray(a, np.int32) for a in (i, j, k))
+        slot = None if slot is None else np.ascontiguousarray(slot, np.int32)
+        _chk(self.L.tfo_load_angles(self.h, len(i), _ip(i), _ip(j), _ip(k), _ip(slot)), "load_angles")
+
+    def step(self, n=1):
+        _chk(self.L.tfo_step(self.h, n), "step")
+
+    def force_only(self, with_bonded=True):
+        _chk(self.L.tfo_force_only(self.h, 1 if with_bonded else 0), "force_only")
+
+    def download(self):
+        n, ns = self.n, self.nspec
+        out = dict(x=np.zeros((n, 3), np.float32), xrel=np.zeros((n, 3), np.float32),
+                   cell=np.zeros(n, np.int32), v=np.zeros((n, 3), np.float32), f=np.zeros((n, 3), np.float32),
+                   density=np.zeros(n, np.float32), species=np.zeros((n, max(ns, 0)), np.float32),
+                   q=np.zeros((n, max(ns, 0)), np.float32))
+        _chk(self.L.tfo_download(self.h, _fp(out["x"]), _fp(out["xrel"]), _ip(out["cell"]), _fp(out["v"]),
+                                 _fp(out["f"]), _fp(out["density"]),
+                                 _fp(out["species"]) if ns else None, _fp(out["q"]) if ns else None), "download")
+        return out
+
+    def forces_f64(self):
+        f = np.zeros((self.n, 4), np.float64)
+        _chk(self.L.tfo_download_forces_f64(self.h, f.ctypes.data_as(C.POINTER(C.c_double))), "forces_f64")
+        return f
+
+    def fmag(self):
+        m = np.zeros(self.n, np.float64)
+        _chk(self.L.tfo_download_fmag(self.h, m.ctypes.data_as(C.POINTER(C.c_double))), "fmag")
+        return m
+
+    def signature(self):
+        """(count, hash) per particle id of the last force pass, accumulated in the pair loop."""
+        cnt = np.zeros(self.n, np.int32)
+        hsh = np.zeros(self.n, np.uint32)
+        _chk(self.L.tfo_signature(self.h, _ip(cnt), _up(hsh)), "signature")
+        return cnt, hsh
+
+    def pair_signature(self):
+        """(count, hash) per particle id from the recorded pair list (same mix as the GPU)."""
+        pr = self.pairs()
+        cnt = np.zeros(self.n, np.int64)
+        hsh = np.zeros(self.n, np.uint64)
+        if len(pr):
+            a, b = pr[:, 0].astype(np.int64), pr[:, 1].astype(np.int64)
+            np.add.at(cnt, a, 1)
+            np.add.at(cnt, b, 1)
+            np.add.at(hsh, a, sig_mix(b))
+            np.add.at(hsh, b, sig_mix(a))
+        return cnt.astype(np.int32), (hsh & 0xFFFFFFFF).astype(np.uint32)
+
+    def reductions(self):
+        r = abi.Reductions()
+        _chk(self.L.tfo_get_reductions(self.h, C.byref(r)), "reductions")
+        return r
+
+    def stats(self):
+        s = (C.c_int64 * 3)()
+        _chk(self.L.tfo_get_stats(self.h, s), "stats")
+        return dict(window_skips=s[0], straight_angles=s[1], tasks=s[2])
+
+    def record_pairs(self, on=True):
+        _chk(self.L.tfo_record_pairs(self.h, 1 if on else 0), "record_pairs")
+
+    def pairs(self):
+        n = self.L.tfo_get_pairs(self.h, None, 0)
+        out = np.zeros((n, 2), np.int32)
+        self.L.tfo_get_pairs(self.h, _ip(out), n)
+        return out
+
+
+def sig_mix(ids):
+    """32-bit mix of particle ids used by the pair signature (uint64 arrays in, out)."""
+    x = (ids.astype(np.uint64) * np.uint64(2654435761) + np.uint64(0x9E3779B9)) & np.uint64(0xFFFFFFFF)
+    x ^= x >> np.uint64(15)
+    x = (x * np.uint64(0x85EBCA6B)) & np.uint64(0xFFFFFFFF)
+    x ^= x >> np.uint64(13)
+    return x
+
+
+def philox(c, k):
+    out = (C.c_uint32 * 4)()
+    lib().tfo_philox_probe(c[0], c[1], c[2], c[3], k[0], k[1], out)
+    return list(out)

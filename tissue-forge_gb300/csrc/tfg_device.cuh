@@ -1,0 +1,186 @@
+// Device-side data layout and per-pair arithmetic of the GB300 engine.
+//
+// Particles are stored structure-of-arrays in cell order (re-binned every step by a
+// counting sort).  All pair arithmetic that decides WHICH pairs interact is done with
+// explicitly rounded FP32 intrinsics (__fadd_rn / __fsub_rn / __fmul_rn), so that it is
+// bit-identical to the reference's scalar build (-mavx -msse4.2, no FMA contraction,
+// CMakeLists.txt:78,91-95): cell-relative coordinates, per-pair shift from the cell
+// origins (space_getsid, tfSpace.cpp:79-114) and r2 = dx.dx (fptype_r2,
+// include/tf_fptype.h:204-210).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "tfg.h"
+
+namespace tfg {
+
+constexpr int kChunk = TFG_POTENTIAL_CHUNK;
+constexpr int kMaxTypes = 16;
+constexpr int kMaxFluxPerPair = TFG_MAX_FLUX_PER_PAIR;
+constexpr int kMaxSpecies = 8;
+constexpr int kMaxBondSlots = 16;
+
+// Error bits set by kernels; the host maps them to TFG_E_* at sync.
+enum : uint32_t {
+    ERR_TOOFAST = 1u << 0,
+    ERR_NAN = 1u << 1,
+    ERR_OVERFLOW = 1u << 2,
+    ERR_RANGE = 1u << 3,
+};
+
+// Random streams (Philox4x32-10 counter word 3).
+enum : uint32_t { STREAM_DPD = 0xD0D0u, STREAM_FORCE = 0xF0F0u, STREAM_ANGLE = 0xA0A0u };
+
+// One potential as consumed by the kernels (struct Potential, tfPotential.h:213-253).
+struct PotDev {
+    uint32_t kind;       // 0 none, 1 table, 2 dpd  (internal encoding, see engine)
+    uint32_t flags;
+    float alpha0, alpha1, alpha2;
+    float r0_plusone, a, b;
+    int32_t n;
+    int32_t offset;      // float offset of the table in the table blob
+    float dpd_alpha, dpd_gamma, dpd_sigma;
+};
+enum : uint32_t { POT_NONE = 0, POT_TABLE = 1, POT_DPD = 2 };
+
+struct FluxDev {
+    int32_t kind, type_a, type_b, index_a, index_b;
+    float coef, half_decay, target, cutoff;
+};
+
+struct FluxSet {
+    int32_t count;
+    FluxDev f[kMaxFluxPerPair];
+};
+
+// Per-step kernel parameters of one simulation.
+struct SimParams {
+    float h[3], dim[3];
+    int32_t cdim[3];
+    int32_t ncells;
+    float cutoff, cutoff2;
+    float dt, dt_flux;
+    float maxx[3], maxx2[3], maxv[3], maxv2[3], h2[3];
+    float self_density;      // W(0, cutoff)
+    float dpd_delta;         // 1/sqrt(dt) in FP32
+    int32_t max_type, nspec;
+    uint32_t flags;          // TFG_ENGINE_*
+    uint64_t seed;
+    int64_t time;            // engine time of the step being computed
+    const float *corig[3];   // cell origin per axis, cdim[k] entries
+};
+
+// ---------------- Philox4x32-10 (Salmon et al., SC'11) ----------------
+struct U4 { uint32_t x, y, z, w; };
+
+__device__ __forceinline__ U4 philox(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        U4 n = {hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        c = n;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// (0,1) uniform from the 24 high bits.
+__device__ __forceinline__ float u01(uint32_t u) {
+    return __fadd_rn(__fmul_rn((float)(u >> 8), 5.9604644775390625e-8f), 2.98023223876953125e-8f);
+}
+
+__device__ __forceinline__ float gauss_pair(uint64_t seed, int64_t step, int ida, int idb) {
+    int lo = min(ida, idb), hi = max(ida, idb);
+    U4 r = philox({(uint32_t)step, (uint32_t)lo, (uint32_t)hi, STREAM_DPD}, (uint32_t)seed, (uint32_t)(seed >> 32));
+    float u1 = u01(r.x), u2 = u01(r.y);
+    return sqrtf(-2.0f * logf(u1)) * cosf(6.283185307179586f * u2);
+}
+
+// ---------------- geometry ----------------
+__device__ __forceinline__ int cell_index(const SimParams &P, int i, int j, int k) {
+    return (i * P.cdim[1] + j) * P.cdim[2] + k;
+}
+
+__device__ __forceinline__ void cell_loc(const SimParams &P, int c, int &i, int &j, int &k) {
+    k = c % P.cdim[2];
+    int t = c / P.cdim[2];
+    j = t % P.cdim[1];
+    i = t / P.cdim[1];
+}
+
+// Shift from cell at loc a to cell at loc b along axis k, wrapped into (-dim/2, dim/2]
+// exactly as space_getsid computes it.
+__device__ __forceinline__ float cell_shift(const SimParams &P, int k, int la, int lb) {
+    float s = __fsub_rn(P.corig[k][lb], P.corig[k][la]);
+    float s2 = __fmul_rn(s, 2.0f);
+    if (s2 > P.dim[k]) s = __fsub_rn(s, P.dim[k]);
+    else if (s2 < -P.dim[k]) s = __fadd_rn(s, P.dim[k]);
+    return s;
+}
+
+// r2 = dx.dx with dx = (xi - shift) - xj, no contraction.
+__device__ __forceinline__ float pair_r2(float3 xi, float3 sh, float3 xj, float3 &dx) {
+    dx.x = __fsub_rn(__fsub_rn(xi.x, sh.x), xj.x);
+    dx.y = __fsub_rn(__fsub_rn(xi.y, sh.y), xj.y);
+    dx.z = __fsub_rn(__fsub_rn(xi.z, sh.z), xj.z);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx.x, dx.x), __fmul_rn(dx.y, dx.y)), __fmul_rn(dx.z, dx.z));
+}
+
+__device__ __forceinline__ float pair_r2_self(float3 xi, float3 xj, float3 &dx) {
+    dx.x = __fsub_rn(xi.x, xj.x);
+    dx.y = __fsub_rn(xi.y, xj.y);
+    dx.z = __fsub_rn(xi.z, xj.z);
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx.x, dx.x), __fmul_rn(dx.y, dx.y)), __fmul_rn(dx.z, dx.z));
+}
+
+// ---------------- per-pair physics ----------------
+// Cubic-spline number density W(r2, h) (tf_smoothing_kernel.h:49-67).  The reference's
+// x86 build takes r from a 12-bit rsqrt estimate; this uses the correctly rounded sqrt.
+__device__ __forceinline__ float density_w(float r2, float h) {
+    float r = __fsqrt_rn(r2);
+    float x = __fdiv_rn(r, h);
+    float y;
+    if (x < 1.f) {
+        float x2 = __fmul_rn(x, x);
+        y = __fadd_rn(__fsub_rn(1.f, __fmul_rn(1.5f, x2)), __fmul_rn(__fmul_rn(0.75f, x2), x));
+    } else if (x < 2.f) {
+        float arg = __fsub_rn(2.f, x);
+        y = __fmul_rn(__fmul_rn(__fmul_rn(0.25f, arg), arg), arg);
+    } else {
+        y = 0.f;
+    }
+    double den = 3.14159265358979323846 * (double)h * (double)h * (double)h;
+    return (float)((double)y / den);
+}
+
+// Tabulated potential (potential_eval_ex, tf_potential_eval.h:104-146).  Returns false
+// when out of range.  The interval index is computed with the reference's unfused FP32
+// arithmetic so the same interval is chosen; the Horner recurrence uses FMA.
+__device__ __forceinline__ bool table_eval(const PotDev &p, const float *__restrict__ blob, float ri, float rj,
+                                           float r2, float &e, float &f) {
+    float r = __fsqrt_rn(r2);
+    float ro = r < 1.1920928955078125e-7f ? 1.1920928955078125e-7f : r;
+    if (p.flags & TFG_POTENTIAL_SCALED) r = __fdiv_rn(r, __fadd_rn(ri, rj));
+    else if (p.flags & TFG_POTENTIAL_SHIFTED) r = __fadd_rn(__fsub_rn(r, __fadd_rn(ri, rj)), p.r0_plusone);
+    r = r < p.a ? p.a : r;
+    float t = __fadd_rn(p.alpha0, __fmul_rn(r, __fadd_rn(p.alpha1, __fmul_rn(r, p.alpha2))));
+    unsigned ind = (unsigned)fmaxf(0.0f, t);
+    if (r > p.b || ind > (unsigned)p.n) return false;
+    const float *c = blob + p.offset + ind * kChunk;
+    float x = (r - c[0]) * c[1];
+    float ee = fmaf(c[2], x, c[3]), eff = c[2];
+#pragma unroll
+    for (int k = 4; k < kChunk; k++) {
+        eff = fmaf(eff, x, ee);
+        ee = fmaf(ee, x, c[k]);
+    }
+    e = ee;
+    f = __fdiv_rn(eff * c[1], ro);
+    return true;
+}
+
+}  // namespace tfg

@@ -1,0 +1,80 @@
+// Host-side engine state and kernel launch entry points shared by the CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "tfg.h"
+#include "tfg_device.cuh"
+
+namespace tfg {
+
+// Per-particle device state, stored in cell order.  Two copies exist so the counting
+// sort can scatter from one into the other.
+struct ParticleArrays {
+    float4 *pos = nullptr;     // cell-relative x,y,z ; w = type (int bits)
+    float4 *vel = nullptr;     // v.x,v.y,v.z ; w = inverse number density
+    float4 *aux = nullptr;     // radius, imass, flags (bits), id (bits)
+    float4 *fext = nullptr;    // force_i (external) ; w unused
+    float4 *pforce = nullptr;  // persistent random force ; w unused
+    int32_t *cell = nullptr;   // cell index of each slot
+    float *sval = nullptr;     // species values, [s * cap + slot]
+    float *sq = nullptr;       // flux increments, [s * cap + slot]
+};
+
+// Reduction slots in the device double array.
+enum RedSlot : int {
+    RED_EPOT_NONBOND = 0,
+    RED_EPOT_BOND,
+    RED_EPOT_ANGLE,
+    RED_KINETIC,
+    RED_VIRIAL,
+    RED_VOLUME,
+    RED_MIGRATIONS,
+    RED_SPECIES0,               // kMaxSpecies entries
+    RED_COUNT = RED_SPECIES0 + kMaxSpecies,
+};
+
+struct PairKernelArgs {
+    SimParams P;
+    int n;
+    const float4 *pos;
+    const float4 *vel;
+    const float4 *aux;
+    const float4 *fext;
+    const float4 *pforce;
+    const int32_t *cell;
+    const int32_t *start;       // ncells+1
+    const float *sval;
+    float *sq;
+    int cap;
+    float4 *force;              // out: f.xyz, number density
+    const PotDev *pots;         // max_type^2
+    const float *blob;
+    int blob_floats;
+    const FluxSet *fluxes;      // max_type^2
+    const float4 *rforce;       // per type: mean, std, duration, enabled
+    float4 *pforce_out;         // persistent force updated in place (same as pforce)
+    double *red;
+    uint32_t *err;
+    int32_t *sig_count;         // signature mode: interacting neighbours per particle
+    uint32_t *sig_hash;         // signature mode: order-independent hash of neighbour ids
+};
+
+void launch_pair(const PairKernelArgs &a, cudaStream_t s);
+// Same stencil walk and pair decision as launch_pair, writing only the per-particle
+// pair signature (used to prove the pair set bit-exact against the oracle).
+void launch_pair_signature(const PairKernelArgs &a, cudaStream_t s);
+
+// Hash of one neighbour id for the pair signature.
+__host__ __device__ inline uint32_t sig_mix(uint32_t id) {
+    uint32_t x = id * 2654435761u + 0x9E3779B9u;
+    x ^= x >> 15;
+    x *= 0x85EBCA6Bu;
+    x ^= x >> 13;
+    return x;
+}
+
+}  // namespace tfg

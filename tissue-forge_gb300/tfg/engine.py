@@ -1,0 +1,196 @@
+"""Python handle of one GB300 engine (libtfg's tfg_engine).
+
+Method names mirror the reference engine's operations: set_potential ~ engine_addpot
+(tfEngine.cpp:1054), add_flux ~ engine_addfluxes (:1079), load ~ space_addpart
+(tfSpace.cpp:477), step ~ engine_step (:1378), force_only ~ engine_force_prep +
+engine_force (:1431-1557).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from ._lib import lib
+from .potentials import Potential
+
+
+class TfgError(RuntimeError):
+    def __init__(self, code, what, msg=""):
+        super().__init__("%s failed: %s %s" % (what, abi.STATUS_NAMES.get(code, code), msg))
+        self.code = code
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(abi.F_P)
+
+
+def _ip(a):
+    return None if a is None else a.ctypes.data_as(abi.I_P)
+
+
+def _up(a):
+    return None if a is None else a.ctypes.data_as(abi.U_P)
+
+
+def _conv(a, dt):
+    return None if a is None else np.ascontiguousarray(a, dt)
+
+
+class Engine:
+    def __init__(self, desc):
+        self.L = lib()
+        self.h = C.c_void_p()
+        self.desc = desc
+        self.nspec = desc.nr_species
+        rc = self.L.tfg_engine_create(C.byref(desc), C.byref(self.h))
+        if rc != 0:
+            raise TfgError(rc, "tfg_engine_create")
+        self.n = 0
+        self._keep = []
+
+    def _chk(self, rc, what):
+        if rc != 0:
+            raise TfgError(rc, what, self.L.tfg_last_error(self.h).decode(errors="replace"))
+
+    def close(self):
+        if self.h:
+            self.L.tfg_engine_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_type(self, t, dynamics, mass=1.0):
+        self._chk(self.L.tfg_set_type(self.h, t, dynamics, mass), "set_type")
+
+    def set_potential(self, ti, tj, pot):
+        ptr = pot.ptr if isinstance(pot, Potential) else pot
+        self._chk(self.L.tfg_set_potential(self.h, ti, tj, ptr), "set_potential")
+
+    def add_flux(self, ti, tj, flux):
+        self._chk(self.L.tfg_add_flux(self.h, ti, tj, C.byref(flux)), "add_flux")
+
+    def set_species_flags(self, flags):
+        a = np.ascontiguousarray(flags, np.uint32)
+        self._chk(self.L.tfg_set_species_flags(self.h, len(a), _up(a)), "set_species_flags")
+
+    def set_random_force(self, t, mean, std, duration_steps):
+        self._chk(self.L.tfg_set_random_force(self.h, t, mean, std, duration_steps), "set_random_force")
+
+    def set_bonded_potential(self, slot, pot):
+        ptr = pot.ptr if isinstance(pot, Potential) else pot
+        self._chk(self.L.tfg_set_bonded_potential(self.h, slot, ptr), "set_bonded_potential")
+
+    def load(self, x, v=None, type=None, radius=None, imass=None, flags=None, species=None, force_i=None):
+        x = np.ascontiguousarray(x, np.float32)
+        self.n = x.shape[0]
+        v, radius, imass, species, force_i = (_conv(a, np.float32) for a in (v, radius, imass, species, force_i))
+        type = _conv(type, np.int32)
+        flags = _conv(flags, np.uint32)
+        self._chk(self.L.tfg_load_particles(self.h, self.n, _fp(x), _fp(v), _ip(type), _fp(radius), _fp(imass),
+                                            _up(flags), _fp(species), _fp(force_i)), "load_particles")
+
+    def load_binned(self, cell, xrel, v=None, type=None, radius=None, imass=None, flags=None, species=None,
+                    force_i=None):
+        cell = np.ascontiguousarray(cell, np.int32)
+        xrel = np.ascontiguousarray(xrel, np.float32)
+        self.n = cell.shape[0]
+        v, radius, imass, species, force_i = (_conv(a, np.float32) for a in (v, radius, imass, species, force_i))
+        type = _conv(type, np.int32)
+        flags = _conv(flags, np.uint32)
+        self._chk(self.L.tfg_load_particles_binned(self.h, self.n, _ip(cell), _fp(xrel), _fp(v), _ip(type),
+                                                   _fp(radius), _fp(imass), _up(flags), _fp(species),
+                                                   _fp(force_i)), "load_particles_binned")
+
+    def load_bonds(self, i, j, slot=None):
+        i, j = (np.ascontiguousarray(a, np.int32) for a in (i, j))
+        slot = _conv(slot, np.int32)
+        self._chk(self.L.tfg_load_bonds(self.h, len(i), _ip(i), _ip(j), _ip(slot)), "load_bonds")
+
+    def load_angles(self, i, j, k, slot=None):
+        i, j, k = (np.ascontiguousarray(a, np.int32) for a in (i, j, k))
+        slot = _conv(slot, np.int32)
+        self._chk(self.L.tfg_load_angles(self.h, len(i), _ip(i), _ip(j), _ip(k), _ip(slot)), "load_angles")
+
+    def step(self, n=1, sync=True):
+        self._chk(self.L.tfg_step(self.h, n), "step")
+        if sync:
+            self.sync()
+
+    def force_only(self, with_bonded=True):
+        self._chk(self.L.tfg_force_only(self.h, 1 if with_bonded else 0), "force_only")
+        self.sync()
+
+    def pair_signature(self):
+        """(count, hash) per particle id of the current binned state's pair set."""
+        cnt = np.zeros(self.n, np.int32)
+        hsh = np.zeros(self.n, np.uint32)
+        self._chk(self.L.tfg_pair_signature(self.h, _ip(cnt), _up(hsh)), "pair_signature")
+        return cnt, hsh
+
+    def set_stream(self, stream_ptr):
+        """Order the engine's work on the caller's CUDA stream (cudaStream_t as int)."""
+        self._chk(self.L.tfg_engine_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
+
+    def sync(self):
+        self._chk(self.L.tfg_sync(self.h), "sync")
+
+    def download(self):
+        n, ns = self.n, self.nspec
+        out = dict(x=np.zeros((n, 3), np.float32), xrel=np.zeros((n, 3), np.float32),
+                   cell=np.zeros(n, np.int32), v=np.zeros((n, 3), np.float32), f=np.zeros((n, 3), np.float32),
+                   density=np.zeros(n, np.float32), species=np.zeros((n, max(ns, 0)), np.float32),
+                   q=np.zeros((n, max(ns, 0)), np.float32))
+        self._chk(self.L.tfg_download(self.h, _fp(out["x"]), _fp(out["xrel"]), _ip(out["cell"]), _fp(out["v"]),
+                                      _fp(out["f"]), _fp(out["density"]),
+                                      _fp(out["species"]) if ns else None, _fp(out["q"]) if ns else None),
+                  "download")
+        return out
+
+    def reductions(self):
+        r = abi.Reductions()
+        self._chk(self.L.tfg_get_reductions(self.h, C.byref(r)), "get_reductions")
+        return r
+
+    def phase_ms(self):
+        ms = (C.c_float * 4)()
+        self._chk(self.L.tfg_get_phase_ms(self.h, ms), "get_phase_ms")
+        return list(ms)
+
+
+def setup_model(eng, w, keep=None):
+    """Apply a configs.Workload's interaction model and particles to an engine-like object
+    (the GPU Engine or the CPU oracle share these method names).  Returns the Potential
+    objects, which must stay alive while the engine uses their tables."""
+    pots = []
+    for t in range(w.max_type):
+        eng.set_type(t, w.dynamics[t], w.mass[t])
+    for (ti, tj), spec in w.pots.items():
+        p = Potential.from_spec(spec)
+        pots.append(p)
+        eng.set_potential(ti, tj, p.ptr)
+    for (ti, tj, f) in w.fluxes:
+        eng.add_flux(ti, tj, f)
+    if w.random_force is not None:
+        mean, std, dur = w.random_force
+        for t in range(w.max_type):
+            eng.set_random_force(t, mean, std, dur)
+    if w.bond_pot is not None:
+        p = Potential.from_spec(w.bond_pot)
+        pots.append(p)
+        eng.set_bonded_potential(0, p.ptr)
+    if w.angle_pot is not None:
+        p = Potential.from_spec(w.angle_pot)
+        pots.append(p)
+        eng.set_bonded_potential(1, p.ptr)
+    eng.load(w.x, v=w.v, type=w.type, radius=w.radius, imass=w.imass, species=w.species)
+    if w.bonds is not None:
+        eng.load_bonds(w.bonds[:, 0], w.bonds[:, 1], np.zeros(len(w.bonds), np.int32))
+    if w.angles is not None:
+        eng.load_angles(w.angles[:, 0], w.angles[:, 1], w.angles[:, 2], np.ones(len(w.angles), np.int32))
+    if keep is not None:
+        keep.extend(pots)
+    return pots
