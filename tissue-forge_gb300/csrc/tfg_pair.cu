@@ -20,7 +20,7 @@ namespace tfg {
 namespace {
 
 constexpr int kPairThreads = 128;
-constexpr int kMaxSmemBlob = 12 * 1024;   // floats of table blob staged in shared memory
+constexpr int kMaxSmemBlob = 8 * 1024;    // floats of table blob staged in shared memory (32 KB)
 
 struct Accum {
     float fx, fy, fz, dens;
