@@ -131,7 +131,7 @@ def cpu_reference_rate(w, threads, budget_s, max_steps=200):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from tfg.engine import setup_model
-    e = O.OracleEngine(w.desc(), 0, threads)
+    e = O.OracleEngine(w.desc(), 0, threads, signature=False)
     keep = setup_model(e, w)
     e.step(1)   # warm-up
     t0 = time.perf_counter()
@@ -217,7 +217,9 @@ def main():
     w = make_workload(args.workload, rank)
     eng = Engine(w.desc(device=dev))
     keep = setup_model(eng, w)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream shared by the engine and the timing events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     eng.set_stream(stream.cuda_stream)
     if w.relax_steps:
         # steepest-descent-like relaxation with the reference's displacement clamp (untimed)

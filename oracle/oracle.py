@@ -72,6 +72,7 @@ def lib():
         L.tfo_get_reductions.argtypes = [E, C.POINTER(abi.Reductions)]
         L.tfo_get_stats.argtypes = [E, C.POINTER(C.c_int64)]
         L.tfo_signature.argtypes = [E, abi.I_P, abi.U_P]
+        L.tfo_enable_signature.argtypes = [E, C.c_int]
         L.tfo_record_pairs.argtypes = [E, C.c_int]
         L.tfo_get_pairs.argtypes = [E, abi.I_P, C.c_int64]
         L.tfo_get_pairs.restype = C.c_int64
@@ -100,12 +101,13 @@ def _chk(rc, what):
 class OracleEngine:
     """CPU restatement of one Tissue Forge engine (space + potentials + fluxes + bonds)."""
 
-    def __init__(self, desc, mode=0, threads=1):
+    def __init__(self, desc, mode=0, threads=1, signature=True):
         self.L = lib()
         self.h = C.c_void_p()
         self.desc = desc
         self.nspec = desc.nr_species
         _chk(self.L.tfo_create(C.byref(desc), mode, threads, C.byref(self.h)), "create")
+        _chk(self.L.tfo_enable_signature(self.h, 1 if signature else 0), "enable_signature")
         self.n = 0
 
     def close(self):

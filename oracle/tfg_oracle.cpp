@@ -155,6 +155,8 @@ template <typename R> struct Engine {
     std::vector<Cell<R>> cells;
     std::vector<Task> tasks;
     std::vector<int> sortflags;
+    std::vector<std::vector<int>> owned;           // task indices per owner cell
+    std::vector<std::vector<int>> colour_classes;  // owner cells that may run concurrently
     int max_type = 1, nspec = 0;
     std::vector<Pot<R>> pots;                    // max_type^2
     std::vector<std::vector<tfg_flux>> fluxes;   // max_type^2
@@ -183,6 +185,7 @@ template <typename R> struct Engine {
     // per-id lookup (rebuilt on demand)
     std::vector<int> where_cell, where_slot;
     std::vector<uint8_t> migrated;  // particle migrated during the last advance (flux deferral)
+    bool want_sig = false;
     std::vector<int32_t> sig_cnt;
     std::vector<uint32_t> sig_hash;
     bool record_pairs = false;
@@ -404,10 +407,12 @@ static inline uint32_t sig_mix(uint32_t id) {
 template <typename R> static void interact(Engine<R> &e, Part<R> &pi, Part<R> &pj, const float *dx,
                                            float r2f, R &epot, double &vir) {
     // per-particle pair signature (each particle's cell is owned by the running task)
-    e.sig_cnt[pi.id]++;
-    e.sig_cnt[pj.id]++;
-    e.sig_hash[pi.id] += sig_mix((uint32_t)pj.id);
-    e.sig_hash[pj.id] += sig_mix((uint32_t)pi.id);
+    if (e.want_sig) {
+        e.sig_cnt[pi.id]++;
+        e.sig_cnt[pj.id]++;
+        e.sig_hash[pi.id] += sig_mix((uint32_t)pj.id);
+        e.sig_hash[pj.id] += sig_mix((uint32_t)pi.id);
+    }
     if (e.record_pairs) {
         std::lock_guard<std::mutex> g(e.pair_mtx);
         e.pairs.push_back({std::min(pi.id, pj.id), std::max(pi.id, pj.id)});
@@ -782,63 +787,70 @@ template <typename R> static void shuffle(Engine<R> &e) {
     }
 }
 
-template <typename R> static void nonbond(Engine<R> &e) {
-    for (int cid = 0; cid < e.ncells; cid++) do_sort(e, cid);
-    R epot = 0;
-    if (e.nthreads <= 1) {
-        for (const Task &t : e.tasks) {
-            if (t.type == 0) do_self(e, t.i, epot);
-            else do_pair(e, t.i, t.j, epot);
-        }
-        e.epot_nonbond = epot;
-        for (auto &c : e.cells) e.virial += c.virial;
+// Parallel for over [0, n) with `threads` workers taking chunks of `chunk` items.
+template <typename F> static void par_for(int threads, size_t n, size_t chunk, F fn) {
+    if (threads <= 1 || n <= chunk) {
+        for (size_t k = 0; k < n; k++) fn(k);
         return;
     }
-    // Threaded runners over the task list with per-cell exclusion (tfRunner.cpp:204-380).
-    std::vector<std::atomic<uint8_t>> taboo(e.ncells);
-    for (auto &t : taboo) t.store(0);
-    std::vector<std::atomic<uint8_t>> done(e.tasks.size());
-    for (auto &d : done) d.store(0);
-    std::mutex qm;
-    size_t first = 0, ndone = 0;
-    std::vector<R> part_epot(e.nthreads, 0);
-    auto worker = [&](int tid) {
-        for (;;) {
-            int pick = -1;
-            {
-                std::lock_guard<std::mutex> g(qm);
-                if (ndone == e.tasks.size()) return;
-                while (first < e.tasks.size() && done[first].load() != 0) first++;
-                size_t lim = std::min(e.tasks.size(), first + 4096);
-                for (size_t k = first; k < lim; k++) {
-                    if (done[k].load() != 0) continue;
-                    const Task &t = e.tasks[k];
-                    if (taboo[t.i].load() || (t.type == 1 && taboo[t.j].load())) continue;
-                    taboo[t.i].store(1);
-                    if (t.type == 1) taboo[t.j].store(1);
-                    done[k].store(2);
-                    pick = (int)k;
-                    break;
-                }
-            }
-            if (pick < 0) { std::this_thread::yield(); continue; }
-            const Task &t = e.tasks[pick];
-            R ep = 0;
-            if (t.type == 0) do_self(e, t.i, ep);
-            else do_pair(e, t.i, t.j, ep);
-            part_epot[tid] += ep;
-            {
-                std::lock_guard<std::mutex> g(qm);
-                taboo[t.i].store(0);
-                if (t.type == 1) taboo[t.j].store(0);
-                ndone++;
-            }
-        }
-    };
+    std::atomic<size_t> next(0);
     std::vector<std::thread> th;
-    for (int t = 0; t < e.nthreads; t++) th.emplace_back(worker, t);
+    int nt = (int)std::min<size_t>(threads, (n + chunk - 1) / chunk);
+    for (int t = 0; t < nt; t++)
+        th.emplace_back([&]() {
+            for (;;) {
+                size_t k0 = next.fetch_add(chunk);
+                if (k0 >= n) return;
+                size_t k1 = std::min(n, k0 + chunk);
+                for (size_t k = k0; k < k1; k++) fn(k);
+            }
+        });
     for (auto &t : th) t.join();
-    for (R v : part_epot) epot += v;
+}
+
+// Colour of a coordinate: residue mod 3 for the first 3*floor(n/3) cells, unique colours
+// for the (at most two) trailing cells, so that equal colours are >= 3 apart with wrap.
+static inline int axis_colour(int x, int n) {
+    int m = 3 * (n / 3);
+    return x < m ? x % 3 : 3 + (x - m);
+}
+
+// Nonbonded pass.  A pair task's owner is its cell_i (the cell whose shift to cell_j is
+// lexicographically positive); an owner touches itself and its 13 forward neighbours,
+// i.e. x in [x, x+1], y and z in [-1, +1].  Owners of one colour class therefore touch
+// disjoint cells and run concurrently without locks; classes run one after another.
+// This gives the reference runners' per-cell exclusion (tfRunner.cpp:204-380) with a
+// deterministic task order.
+template <typename R> static void nonbond(Engine<R> &e) {
+    par_for(e.nthreads, (size_t)e.ncells, 64, [&](size_t cid) { do_sort(e, (int)cid); });
+    if (e.owned.empty()) {
+        e.owned.assign(e.ncells, std::vector<int>());
+        for (size_t k = 0; k < e.tasks.size(); k++) e.owned[e.tasks[k].i].push_back((int)k);
+        std::vector<std::vector<int>> cls(125);
+        for (int c = 0; c < e.ncells; c++) {
+            const int *l = e.cells[c].loc;
+            int col = (axis_colour(l[0], e.cdim[0]) * 5 + axis_colour(l[1], e.cdim[1])) * 5 +
+                      axis_colour(l[2], e.cdim[2]);
+            cls[col].push_back(c);
+        }
+        for (auto &v : cls)
+            if (!v.empty()) e.colour_classes.push_back(v);
+    }
+    std::vector<R> cell_epot(e.ncells, (R)0);
+    for (const auto &cls : e.colour_classes) {
+        par_for(e.nthreads, cls.size(), 8, [&](size_t q) {
+            int owner = cls[q];
+            R ep = 0;
+            for (int k : e.owned[owner]) {
+                const Task &t = e.tasks[k];
+                if (t.type == 0) do_self(e, t.i, ep);
+                else do_pair(e, t.i, t.j, ep);
+            }
+            cell_epot[owner] = ep;
+        });
+    }
+    R epot = 0;
+    for (R v : cell_epot) epot += v;
     e.epot_nonbond = epot;
     for (auto &c : e.cells) e.virial += c.virial;
 }
@@ -1313,6 +1325,12 @@ TFG_API int tfo_get_reductions(tfo_engine *eh, tfg_reductions *out) {
         out->migrations = e.migrations;
         return TFG_OK;
     };
+    return DISPATCH(h, go);
+}
+
+TFG_API int tfo_enable_signature(tfo_engine *eh, int on) {
+    Handle *h = reinterpret_cast<Handle *>(eh);
+    auto go = [&](auto &e) { e.want_sig = on != 0; return TFG_OK; };
     return DISPATCH(h, go);
 }
 

@@ -139,10 +139,10 @@ __device__ __forceinline__ float pair_r2_self(float3 xi, float3 xj, float3 &dx) 
 
 // ---------------- per-pair physics ----------------
 // Cubic-spline number density W(r2, h) (tf_smoothing_kernel.h:49-67).  The reference's
-// x86 build takes r from a 12-bit rsqrt estimate; this uses the correctly rounded sqrt.
-__device__ __forceinline__ float density_w(float r2, float h) {
-    float r = __fsqrt_rn(r2);
-    float x = __fdiv_rn(r, h);
+// x86 build takes r from a 12-bit rsqrt estimate; this uses the correctly rounded sqrt
+// (computed once per pair by the caller), r/h as r*(1/h) and y/(pi h^3) as y*norm.
+__device__ __forceinline__ float density_w(float r, float inv_h, float norm) {
+    float x = r * inv_h;
     float y;
     if (x < 1.f) {
         float x2 = __fmul_rn(x, x);
@@ -153,8 +153,7 @@ __device__ __forceinline__ float density_w(float r2, float h) {
     } else {
         y = 0.f;
     }
-    double den = 3.14159265358979323846 * (double)h * (double)h * (double)h;
-    return (float)((double)y / den);
+    return y * norm;   // norm = 1 / (pi h^3)
 }
 
 // Tabulated potential (potential_eval_ex, tf_potential_eval.h:104-146).  Returns false

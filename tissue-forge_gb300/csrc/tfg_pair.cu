@@ -25,7 +25,7 @@ constexpr int kMaxSmemBlob = 8 * 1024;    // floats of table blob staged in shar
 struct Accum {
     float fx, fy, fz, dens;
     float q[kMaxSpecies];
-    double epot, vir;
+    float epot, vir;     // per-thread partial sums; FP64 only in the block reduction
 };
 
 template <bool kHasFlux>
@@ -96,8 +96,9 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
     acc.dens = P.self_density;
 #pragma unroll
     for (int s = 0; s < kMaxSpecies; s++) acc.q[s] = 0.f;
-    acc.epot = 0.0;
-    acc.vir = 0.0;
+    acc.epot = 0.f;
+    acc.vir = 0.f;
+    const float inv_cut = 1.0f / P.cutoff;
 
     // Gaussian single-body force (gaussian_force, tfForce.cpp:211-223), applied in the
     // reference from runner_doself before the pair loop.
@@ -170,10 +171,10 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
                 sig_h += sig_mix((uint32_t)__float_as_int(a.aux[j].w));
                 continue;
             }
-            if (kDensity) acc.dens += density_w(r2, P.cutoff);
+            const float r = __fsqrt_rn(r2);
+            if (kDensity) acc.dens += density_w(r, inv_cut, P.self_density);
             const int tj = __float_as_int(pj4.w);
             const int pidx = ti * P.max_type + tj;
-            const float r = __fsqrt_rn(r2);
             if (kHasFlux) {
                 const FluxSet &fs = a.fluxes[pidx];
                 if (fs.count) pair_flux<kHasFlux>(a, fs, i_is_pi, ti, tj, i, j, r, acc);
@@ -188,8 +189,8 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
                     acc.fx += sgn * (f * dx.x);
                     acc.fy += sgn * (f * dx.y);
                     acc.fz += sgn * (f * dx.z);
-                    acc.epot += 0.5 * (double)e;
-                    acc.vir += -0.5 * (double)f * (double)r2;
+                    acc.epot += 0.5f * e;
+                    acc.vir -= 0.5f * f * r2;
                 }
             } else if (pot.kind == POT_DPD) {
                 const float4 axj = a.aux[j];
@@ -219,7 +220,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
                     acc.fx += sgn * (ftot * ev.x);
                     acc.fy += sgn * (ftot * ev.y);
                     acc.fz += sgn * (ftot * ev.z);
-                    acc.vir += 0.5 * (double)ftot * (double)ro;
+                    acc.vir += 0.5f * ftot * ro;
                 }
             }
         }
@@ -233,8 +234,8 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
         if (kHasFlux) {
             for (int s = 0; s < P.nspec; s++) a.sq[s * a.cap + i] += acc.q[s];
         }
-        red_epot = acc.epot;
-        red_vir = acc.vir;
+        red_epot = (double)acc.epot;
+        red_vir = (double)acc.vir;
     }
     }  // i < n
     if (kSig) return;
