@@ -49,6 +49,9 @@ struct tfg_engine {
     int bblob_cap = 0;
     double *red = nullptr;
     uint32_t *err = nullptr;
+    int *overflow_list = nullptr, *overflow_count = nullptr;
+    int sms = 1;
+    bool has_dpd = false, has_flux = false;
     uint32_t *species_flags = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -239,17 +242,43 @@ __global__ void k_rank(int ncells, const int32_t *start, const int32_t *tmp_id, 
     }
 }
 
+// Scatter into cell order and initialise the force of the coming pair pass: f = force_i
+// plus the Gaussian persistent force (gaussian_force, tfForce.cpp:211-223, redrawn when
+// (time + id) % duration == 0 from a Philox stream) and f[3] = W(0) (space_prepare,
+// tfSpace.cpp:182-201).
 __global__ void k_scatter(int n, int cap, int nspec, const int32_t *dest, ParticleArrays src, ParticleArrays dst,
-                          const int32_t *cell_src, int32_t *slot_of_id) {
+                          const int32_t *cell_src, int32_t *slot_of_id, SimParams P, const float4 *rforce,
+                          float4 *force) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int d = dest[i];
     float4 ax = src.aux[i];
-    dst.pos[d] = src.pos[i];
+    const float4 p = src.pos[i];
+    const float4 fe = src.fext[i];
+    float4 pf = src.pforce[i];
+    const int id = __float_as_int(ax.w);
+    const float4 rf = rforce[__float_as_int(p.w)];
+    if (rf.w != 0.f) {
+        const int dur = (int)rf.z;
+        if ((P.time + id) % dur == 0) {
+            U4 r = philox({(uint32_t)P.time, (uint32_t)id, 0u, STREAM_FORCE}, (uint32_t)P.seed, (uint32_t)(P.seed >> 32));
+            const float theta = 6.283185307179586f * u01(r.x);
+            const float phi = acosf(1.f - 2.f * u01(r.y));
+            const float g = sqrtf(-2.0f * logf(u01(r.z))) * cosf(6.283185307179586f * u01(r.w));
+            const float rr = rf.x + rf.y * g;
+            pf.x = rr * sinf(phi) * cosf(theta);
+            pf.y = rr * sinf(phi) * sinf(theta);
+            pf.z = rr * cosf(phi);
+        }
+        force[d] = make_float4(fe.x + pf.x, fe.y + pf.y, fe.z + pf.z, P.self_density);
+    } else {
+        force[d] = make_float4(fe.x, fe.y, fe.z, P.self_density);
+    }
+    dst.pos[d] = p;
     dst.vel[d] = src.vel[i];
     dst.aux[d] = ax;
-    dst.fext[d] = src.fext[i];
-    dst.pforce[d] = src.pforce[i];
+    dst.fext[d] = fe;
+    dst.pforce[d] = pf;
     dst.cell[d] = cell_src[i];
     for (int s = 0; s < nspec; s++) {
         dst.sval[s * cap + d] = src.sval[s * cap + i];
@@ -544,6 +573,12 @@ int alloc_particles(tfg_engine *eng, int cap) {
 int upload_tables(tfg_engine *eng) {
     if (!eng->tables_dirty) return TFG_OK;
     const int T = eng->P.max_type;
+    eng->has_dpd = false;
+    eng->has_flux = false;
+    for (int k = 0; k < T * T; k++) {
+        if (eng->h_pots[k].kind == POT_DPD) eng->has_dpd = true;
+        if (eng->h_fluxes[k].count > 0) eng->has_flux = true;
+    }
     // nonbonded blob
     std::vector<float> blob;
     std::vector<PotDev> pots = eng->h_pots;
@@ -625,7 +660,7 @@ int bin(tfg_engine *eng, int shuffle) {
         k_place<<<blocks_for(n), kThreads, 0, s>>>(n, S.cell, eng->lidx, eng->start, S.aux, eng->tmp_id, eng->tmp_src);
         k_rank<<<blocks_for(nc * 32), kThreads, 0, s>>>(nc, eng->start, eng->tmp_id, eng->tmp_src, eng->dest);
         k_scatter<<<blocks_for(n), kThreads, 0, s>>>(n, eng->cap, eng->P.nspec, eng->dest, S, D, S.cell,
-                                                     eng->slot_of_id);
+                                                     eng->slot_of_id, eng->P, eng->rforce, eng->force);
     }
     eng->cur ^= 1;
     return TFG_OK;
@@ -662,14 +697,20 @@ PairKernelArgs pair_args(tfg_engine *eng) {
     a.pforce_out = A.pforce;
     a.red = eng->red;
     a.err = eng->err;
+    a.has_dpd = eng->has_dpd;
+    a.has_flux = eng->has_flux;
     return a;
 }
+
+// The tiled half-shell kernel handles at most one species; more go to the stencil kernel.
+bool use_tile(const tfg_engine *eng) { return !(eng->has_flux && eng->P.nspec > 1); }
 
 int force_pass(tfg_engine *eng, bool bonded, bool timed) {
     cudaStream_t s = eng->stream;
     ParticleArrays &A = eng->A[eng->cur];
     PairKernelArgs a = pair_args(eng);
-    launch_pair(a, s);
+    if (use_tile(eng)) launch_pair_tile(a, eng->overflow_list, eng->overflow_count, eng->sms, false, s);
+    else launch_pair(a, s);
     if (timed) cudaEventRecord(eng->ev[2], s);
     if (bonded) {
         if (eng->nb > 0)
@@ -752,6 +793,7 @@ TFG_API int tfg_engine_create(const tfg_engine_desc *d, tfg_engine **out) {
     if (!eng) return TFG_E_OOM;
     eng->desc = *d;
     if (cudaSetDevice(d->device) != cudaSuccess) { delete eng; return TFG_E_CUDA; }
+    cudaDeviceGetAttribute(&eng->sms, cudaDevAttrMultiProcessorCount, d->device);
     SimParams &P = eng->P;
     for (int k = 0; k < 3; k++) {
         P.dim[k] = d->dim[k];
@@ -795,7 +837,8 @@ TFG_API int tfg_engine_create(const tfg_engine_desc *d, tfg_engine **out) {
         (rc = dalloc(eng, &eng->rforce, T)) || (rc = dalloc(eng, &eng->type_mass, T)) ||
         (rc = dalloc(eng, &eng->type_dyn, T)) || (rc = dalloc(eng, &eng->bpots, kMaxBondSlots)) ||
         (rc = dalloc(eng, &eng->red, RED_COUNT)) || (rc = dalloc(eng, &eng->err, 1)) ||
-        (rc = dalloc(eng, &eng->species_flags, kMaxSpecies))) {
+        (rc = dalloc(eng, &eng->species_flags, kMaxSpecies)) || (rc = dalloc(eng, &eng->overflow_list, P.ncells)) ||
+        (rc = dalloc(eng, &eng->overflow_count, 1))) {
         tfg_engine_destroy(eng);
         return rc;
     }
@@ -835,7 +878,7 @@ TFG_API int tfg_engine_destroy(tfg_engine *eng) {
     void *bufs[] = {eng->force, eng->count, eng->start, eng->lidx, eng->tmp_id, eng->tmp_src, eng->dest,
                     eng->slot_of_id, eng->scan_sums, eng->corig, eng->pots, eng->blob, eng->fluxes, eng->rforce,
                     eng->type_mass, eng->type_dyn, eng->bonds, eng->bond_slot, eng->angles, eng->bpots, eng->bblob,
-                    eng->red, eng->err, eng->species_flags};
+                    eng->red, eng->err, eng->species_flags, eng->overflow_list, eng->overflow_count};
     for (void *p : bufs) cudaFree(p);
     for (int k = 0; k < 5; k++) if (eng->ev[k]) cudaEventDestroy(eng->ev[k]);
     if (eng->own_stream && eng->stream) cudaStreamDestroy(eng->stream);
@@ -1120,7 +1163,9 @@ TFG_API int tfg_pair_signature(tfg_engine *eng, int32_t *count, uint32_t *hash) 
     PairKernelArgs a = pair_args(eng);
     a.sig_count = dbuf;
     a.sig_hash = reinterpret_cast<uint32_t *>(dbuf + n);
-    launch_pair_signature(a, eng->stream);
+    cudaMemsetAsync(dbuf, 0, sizeof(int32_t) * 2 * n, eng->stream);
+    if (use_tile(eng)) launch_pair_tile(a, eng->overflow_list, eng->overflow_count, eng->sms, true, eng->stream);
+    else launch_pair_signature(a, eng->stream);
     cudaMemcpyAsync(count, a.sig_count, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, eng->stream);
     cudaMemcpyAsync(hash, a.sig_hash, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, eng->stream);
     cudaError_t e = cudaStreamSynchronize(eng->stream);

@@ -61,9 +61,18 @@ struct PairKernelArgs {
     uint32_t *err;
     int32_t *sig_count;         // signature mode: interacting neighbours per particle
     uint32_t *sig_hash;         // signature mode: order-independent hash of neighbour ids
+    bool has_dpd;               // any type pair uses a DPD potential
+    bool has_flux;              // any type pair has fluxes
 };
 
+// Full-stencil kernel: one thread per particle, no atomics.  General path (any number
+// of species); force[] must hold the initial force (external + random, density W(0)).
 void launch_pair(const PairKernelArgs &a, cudaStream_t s);
+// Tiled half-shell kernel (one species at most) plus its overflow pass; force[] must hold
+// the initial force, to which both partners' contributions are added atomically.
+void launch_pair_tile(const PairKernelArgs &a, int *overflow_list, int *overflow_count, int sms, bool signature,
+                      cudaStream_t s);
+int pair_tile_capacity();
 // Same stencil walk and pair decision as launch_pair, writing only the per-particle
 // pair signature (used to prove the pair set bit-exact against the oracle).
 void launch_pair_signature(const PairKernelArgs &a, cudaStream_t s);

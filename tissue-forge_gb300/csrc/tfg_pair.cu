@@ -90,38 +90,16 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
 
     Accum acc;
     {
-        const float4 fe = a.fext[i];
-        acc.fx = fe.x; acc.fy = fe.y; acc.fz = fe.z;
+        // initial force: external + random force and the self density W(0), set by the scatter
+        const float4 f0 = a.force[i];
+        acc.fx = f0.x; acc.fy = f0.y; acc.fz = f0.z;
+        acc.dens = f0.w;
     }
-    acc.dens = P.self_density;
 #pragma unroll
     for (int s = 0; s < kMaxSpecies; s++) acc.q[s] = 0.f;
     acc.epot = 0.f;
     acc.vir = 0.f;
     const float inv_cut = 1.0f / P.cutoff;
-
-    // Gaussian single-body force (gaussian_force, tfForce.cpp:211-223), applied in the
-    // reference from runner_doself before the pair loop.
-    if (!kSig) {
-        const float4 rf = a.rforce[ti];
-        if (rf.w != 0.f) {
-            float4 pf = a.pforce[i];
-            const int dur = (int)rf.z;
-            if ((P.time + idi) % dur == 0) {
-                U4 r = philox({(uint32_t)P.time, (uint32_t)idi, 0u, STREAM_FORCE}, (uint32_t)P.seed,
-                              (uint32_t)(P.seed >> 32));
-                float theta = 6.283185307179586f * u01(r.x);
-                float phi = acosf(1.f - 2.f * u01(r.y));
-                float g = sqrtf(-2.0f * logf(u01(r.z))) * cosf(6.283185307179586f * u01(r.w));
-                float rr = rf.x + rf.y * g;
-                pf.x = rr * sinf(phi) * cosf(theta);
-                pf.y = rr * sinf(phi) * sinf(theta);
-                pf.z = rr * cosf(phi);
-                a.pforce_out[i] = pf;
-            }
-            acc.fx += pf.x; acc.fy += pf.y; acc.fz += pf.z;
-        }
-    }
 
     int sig_n = 0;
     uint32_t sig_h = 0;
