@@ -229,6 +229,7 @@ def main():
         for t in range(w.max_type):
             eng.set_type(t, w.dynamics[t], w.mass[t])
 
+    split = eng.autotune()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
         eng.step(1, sync=False)
@@ -303,7 +304,7 @@ def main():
         hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
     except Exception:
         hbm = 6800.0
-    roof = {"bound": "fp32", "kernel": "k_pair_stencil", "achieved": achieved, "peak": peak.value,
+    roof = {"bound": "fp32", "kernel": "k_pair_tile (split %d)" % split, "achieved": achieved, "peak": peak.value,
             "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
             "peak_source": "measured live (tfg_probe_fp32_tflops, FFMA chains)",
             "flops_per_launch": fl_pair, "pairs_per_step": pairs, "flops_per_pair": pair_flops(w),
@@ -327,7 +328,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"],
                        "n_particles": w.n, "cells": list(w.cells), "l2": "flushed between timed steps (256 MiB write)",
-                       "parallelism": "replicas%d" % world,
+                       "parallelism": "replicas%d" % world, "pair_split": split,
                        "phase_ms_per_step": dict(zip(["bin", "pair", "bonded", "advance"],
                                                      (phase_tot / args.steps).round(5).tolist()))},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),

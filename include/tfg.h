@@ -228,6 +228,13 @@ TFG_API int tfg_step(tfg_engine *eng, int nsteps);
  * forces, without the advance.  Leaves f, number density and flux increments readable. */
 TFG_API int tfg_force_only(tfg_engine *eng, int with_bonded);
 TFG_API int tfg_sync(tfg_engine *eng);
+/* Autotune the nonbonded pass's work split (warps per home cell: 1, 2, 7 or 14) by timing
+ * each choice on the current state; the state is left unchanged.  tfg_step and
+ * tfg_force_only run it on their first call; tfg_set_split fixes the split instead.
+ * The reference selects CUDA blocks/threads by hand (cuda::EngineConfig::setBlocks /
+ * setThreads, source/cuda/tfEngineConfig.cpp:98-124). */
+TFG_API int tfg_autotune(tfg_engine *eng, int *split);
+TFG_API int tfg_set_split(tfg_engine *eng, int split);
 /* Pair-set signature of the current binned state, per particle id: the number of
  * partners with r2 <= cutoff^2 and the wrap-around sum of a 32-bit mix of their ids.
  * It runs the pair pass's own stencil walk and pair decision (no forces).  Call it after

@@ -64,6 +64,33 @@ def test_forces_density_flux_match_oracle(wl):
         assert np.max(np.abs(a["q"] - b["q"]) / q_scale) < 1e-4
 
 
+@pytest.mark.parametrize("split", [1, 2, 7, 14])
+def test_every_work_split_matches(split):
+    """Each work split of the tiled pass (warps per home cell) gives the same pair set and
+    forces within tolerance."""
+    w = configs.cell_sorting()
+    g = make_gpu(w)
+    g.set_split(split)
+    o = make_oracle(w)
+    g.force_only()
+    o.force_only()
+    gc, gh = g.pair_signature()
+    oc, oh = o.signature()
+    assert np.array_equal(gc, oc) and np.array_equal(gh, oh)
+    assert force_error(g.download()["f"], o.download()["f"], o.fmag()) < FORCE_RTOL
+
+
+def test_autotune_leaves_state_unchanged():
+    w = small_dpd()
+    g = make_gpu(w)
+    before = g.download()
+    split = g.autotune()
+    assert split in (1, 2, 7, 14)
+    after = g.download()
+    for k in ("x", "v", "species", "q", "cell"):
+        assert np.array_equal(before[k], after[k]), k
+
+
 def test_forces_vs_fp64_oracle(wl):
     """The FP32 GPU forces against the FP64 evaluation of the same tables and pair set."""
     name, w = wl

@@ -51,6 +51,7 @@ struct tfg_engine {
     uint32_t *err = nullptr;
     int *overflow_list = nullptr, *overflow_count = nullptr;
     int sms = 1;
+    int split = 0;          // warps per home cell of the tiled pair kernel (0 = not tuned yet)
     bool has_dpd = false, has_flux = false;
     uint32_t *species_flags = nullptr;
     cudaStream_t stream = nullptr;
@@ -709,7 +710,7 @@ int force_pass(tfg_engine *eng, bool bonded, bool timed) {
     cudaStream_t s = eng->stream;
     ParticleArrays &A = eng->A[eng->cur];
     PairKernelArgs a = pair_args(eng);
-    if (use_tile(eng)) launch_pair_tile(a, eng->overflow_list, eng->overflow_count, eng->sms, false, s);
+    if (use_tile(eng)) launch_pair_tile(a, eng->overflow_list, eng->overflow_count, eng->sms, false, eng->split, s);
     else launch_pair(a, s);
     if (timed) cudaEventRecord(eng->ev[2], s);
     if (bonded) {
@@ -722,6 +723,50 @@ int force_pass(tfg_engine *eng, bool bonded, bool timed) {
                                                              eng->slot_of_id, A.pos, A.cell, eng->force, eng->red);
     }
     if (timed) cudaEventRecord(eng->ev[3], s);
+    return check_launch(eng);
+}
+
+// Pick the tiled pair kernel's work split (warps per home cell) by timing each choice on
+// the current binned state.  Every trial re-initialises the forces with a non-shuffling
+// re-bin (idempotent on sorted data); the flux increments the trials add are saved and
+// restored, so the engine state is unchanged.
+int autotune(tfg_engine *eng) {
+    if (!use_tile(eng) || eng->n == 0) {
+        eng->split = 1;
+        return TFG_OK;
+    }
+    cudaStream_t s = eng->stream;
+    const size_t nq = (size_t)eng->cap * std::max(1, eng->P.nspec);
+    float *save = nullptr;
+    int rc = dalloc(eng, &save, nq);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(save, eng->A[eng->cur].sq, sizeof(float) * nq, cudaMemcpyDeviceToDevice, s));
+    const int cand[4] = {1, 2, 7, 14};
+    float best = 1e30f;
+    int best_split = 1;
+    for (int c = 0; c < 4; c++) {
+        float tmin = 1e30f;
+        for (int rep = 0; rep < 3; rep++) {
+            rc = bin(eng, 0);
+            if (rc) { cudaFree(save); return rc; }
+            PairKernelArgs a = pair_args(eng);
+            cudaEventRecord(eng->ev[0], s);
+            launch_pair_tile(a, eng->overflow_list, eng->overflow_count, eng->sms, false, cand[c], s);
+            cudaEventRecord(eng->ev[1], s);
+            CK(cudaEventSynchronize(eng->ev[1]));
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, eng->ev[0], eng->ev[1]);
+            tmin = std::min(tmin, ms);
+        }
+        if (tmin < best) { best = tmin; best_split = cand[c]; }
+    }
+    CK(cudaMemcpyAsync(eng->A[eng->cur].sq, save, sizeof(float) * nq, cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    cudaFree(save);
+    rc = bin(eng, 0);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s));
+    eng->split = best_split;
     return check_launch(eng);
 }
 
@@ -1125,11 +1170,28 @@ TFG_API int tfg_load_angles(tfg_engine *eng, int n, const int32_t *i, const int3
     return TFG_OK;
 }
 
+TFG_API int tfg_autotune(tfg_engine *eng, int *split) {
+    if (!eng) return TFG_E_INVAL;
+    if (eng->cap == 0) return fail(eng, TFG_E_STATE, "no particles loaded");
+    int rc = upload_tables(eng);
+    if (rc) return rc;
+    rc = autotune(eng);
+    if (split) *split = eng->split;
+    return rc;
+}
+
+TFG_API int tfg_set_split(tfg_engine *eng, int split) {
+    if (!eng || !(split == 1 || split == 2 || split == 7 || split == 14)) return TFG_E_INVAL;
+    eng->split = split;
+    return TFG_OK;
+}
+
 TFG_API int tfg_step(tfg_engine *eng, int nsteps) {
     if (!eng || nsteps < 0) return TFG_E_INVAL;
     if (eng->cap == 0) return fail(eng, TFG_E_STATE, "no particles loaded");
     int rc = upload_tables(eng);
     if (rc) return rc;
+    if (eng->split == 0 && (rc = autotune(eng))) return rc;
     for (int k = 0; k < nsteps; k++) {
         rc = one_step(eng, true, k == nsteps - 1);
         if (rc) return rc;
@@ -1142,6 +1204,7 @@ TFG_API int tfg_force_only(tfg_engine *eng, int with_bonded) {
     if (eng->cap == 0) return fail(eng, TFG_E_STATE, "no particles loaded");
     int rc = upload_tables(eng);
     if (rc) return rc;
+    if (eng->split == 0 && (rc = autotune(eng))) return rc;
     cudaStream_t s = eng->stream;
     eng->time += 1;
     eng->P.time = eng->time;
@@ -1157,6 +1220,7 @@ TFG_API int tfg_pair_signature(tfg_engine *eng, int32_t *count, uint32_t *hash) 
     if (n == 0) return TFG_OK;
     int rc = upload_tables(eng);
     if (rc) return rc;
+    if (eng->split == 0) eng->split = 1;
     int32_t *dbuf = nullptr;
     rc = dalloc(eng, &dbuf, (size_t)2 * n);
     if (rc) return rc;
@@ -1164,7 +1228,8 @@ TFG_API int tfg_pair_signature(tfg_engine *eng, int32_t *count, uint32_t *hash) 
     a.sig_count = dbuf;
     a.sig_hash = reinterpret_cast<uint32_t *>(dbuf + n);
     cudaMemsetAsync(dbuf, 0, sizeof(int32_t) * 2 * n, eng->stream);
-    if (use_tile(eng)) launch_pair_tile(a, eng->overflow_list, eng->overflow_count, eng->sms, true, eng->stream);
+    if (use_tile(eng))
+        launch_pair_tile(a, eng->overflow_list, eng->overflow_count, eng->sms, true, eng->split, eng->stream);
     else launch_pair_signature(a, eng->stream);
     cudaMemcpyAsync(count, a.sig_count, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, eng->stream);
     cudaMemcpyAsync(hash, a.sig_hash, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, eng->stream);

@@ -70,8 +70,10 @@ struct PairKernelArgs {
 void launch_pair(const PairKernelArgs &a, cudaStream_t s);
 // Tiled half-shell kernel (one species at most) plus its overflow pass; force[] must hold
 // the initial force, to which both partners' contributions are added atomically.
+// `split` = warps per home cell (1, 2, 7 or 14): the cell's 14 tasks are divided into
+// that many work items.
 void launch_pair_tile(const PairKernelArgs &a, int *overflow_list, int *overflow_count, int sms, bool signature,
-                      cudaStream_t s);
+                      int split, cudaStream_t s);
 int pair_tile_capacity();
 // Same stencil walk and pair decision as launch_pair, writing only the per-particle
 // pair signature (used to prove the pair set bit-exact against the oracle).

@@ -57,19 +57,22 @@ struct TileArgs {
     PairKernelArgs a;
     int *overflow_list;    // home cells handed to the overflow kernel
     int *overflow_count;
+    int split;             // warps per home cell: the 14 tasks are divided into `split` groups
 };
 
 // Evaluate one interacting pair (reference orientation: I = part_i, J = part_j) and
 // accumulate into the staged accumulators of both.
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
 __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, StagedDyn &D, const PotDev *pots,
-                                          const float *blob, int I, int J, float3 sh, float &epot, float &vir) {
+                                          const float *blob, int I, int J, float3 sh, float &epot, float &vir,
+                                          float4 &fI) {
     const PairKernelArgs &a = T.a;
     const SimParams &P = a.P;
     const float4 pi = S.pos[I], pj = S.pos[J];
     float3 dx;
     const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z), sh, make_float3(pj.x, pj.y, pj.z), dx);
     if (kSig) {
+        // counters live in the accumulator bits: x = count, y = hash (integer atomics)
         atomicAdd(reinterpret_cast<int *>(&S.acc[I].x), 1);
         atomicAdd(reinterpret_cast<int *>(&S.acc[J].x), 1);
         atomicAdd(reinterpret_cast<unsigned *>(&S.acc[I].y), sig_mix((uint32_t)__float_as_int(S.rid[J].y)));
@@ -79,7 +82,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, StagedDy
     const float r = __fsqrt_rn(r2);
     if (kDensity) {
         const float w = density_w(r, 1.0f / P.cutoff, P.self_density);
-        atomicAdd(&S.acc[I].w, w);
+        fI.w += w;
         atomicAdd(&S.acc[J].w, w);
     }
     const int ti = __float_as_int(pi.w), tj = __float_as_int(pj.w);
@@ -114,9 +117,9 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, StagedDy
         float e, f;
         if (table_eval(pot, blob, S.rid[I].x, S.rid[J].x, r2, e, f)) {
             const float wx = f * dx.x, wy = f * dx.y, wz = f * dx.z;
-            atomicAdd(&S.acc[I].x, -wx);
-            atomicAdd(&S.acc[I].y, -wy);
-            atomicAdd(&S.acc[I].z, -wz);
+            fI.x -= wx;
+            fI.y -= wy;
+            fI.z -= wz;
             atomicAdd(&S.acc[J].x, wx);
             atomicAdd(&S.acc[J].y, wy);
             atomicAdd(&S.acc[J].z, wz);
@@ -141,14 +144,46 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, StagedDy
                                pot.dpd_sigma * omega_c * xi_r * P.dpd_delta;
             const float wx = ftot * ex, wy = ftot * ey, wz = ftot * ez;
             // part_i.f += F e ; part_j.f -= F e
-            atomicAdd(&S.acc[I].x, wx);
-            atomicAdd(&S.acc[I].y, wy);
-            atomicAdd(&S.acc[I].z, wz);
+            fI.x += wx;
+            fI.y += wy;
+            fI.z += wz;
             atomicAdd(&S.acc[J].x, -wx);
             atomicAdd(&S.acc[J].y, -wy);
             atomicAdd(&S.acc[J].z, -wz);
             vir += ftot * ro;
         }
+    }
+}
+
+// Evaluate the queued pairs held by the active lanes (entries in enumeration order, so
+// equal I form contiguous runs).  The I side is reduced over each run with a segmented
+// warp scan and written once per distinct I by the run's last lane; the J side (rarely
+// repeated inside a batch) uses shared-memory atomics.
+template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
+__device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, StagedDyn &D, const PotDev *pots,
+                                           const float *blob, bool active, uint32_t e, float3 sh, int lane,
+                                           float &epot, float &vir) {
+    const int I = e & 0xffff, J = e >> 16;
+    float4 fI = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) eval_pair<kDPD, kFlux, kDensity, kSig>(T, S, D, pots, blob, I, J, sh, epot, vir, fI);
+    if (kSig) return;
+    const int key = active ? I : 1024 + lane;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int k2 = __shfl_up_sync(0xffffffffu, key, o);
+        const float x = __shfl_up_sync(0xffffffffu, fI.x, o);
+        const float y = __shfl_up_sync(0xffffffffu, fI.y, o);
+        const float z = __shfl_up_sync(0xffffffffu, fI.z, o);
+        const float w = __shfl_up_sync(0xffffffffu, fI.w, o);
+        if (lane >= o && k2 == key) {
+            fI.x += x; fI.y += y; fI.z += z; fI.w += w;
+        }
+    }
+    const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+    if (active && (lane == 31 || knext != key)) {
+        float4 v = S.acc[I];
+        v.x += fI.x; v.y += fI.y; v.z += fI.z; v.w += fI.w;
+        S.acc[I] = v;
     }
 }
 
@@ -217,7 +252,10 @@ __global__ void __launch_bounds__(kWarps * 32) k_pair_tile(TileArgs T) {
     float epot = 0.f, vir = 0.f;
     const int nwarps_total = gridDim.x * kWarps;
 
-    for (int home = blockIdx.x * kWarps + wid; home < P.ncells; home += nwarps_total) {
+    const int per = 14 / T.split;                       // tasks per work item
+    const int nitems = P.ncells * T.split;
+    for (int item = blockIdx.x * kWarps + wid; item < nitems; item += nwarps_total) {
+        const int home = item / T.split, grp = item - home * T.split;
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         if (nh == 0) continue;
         int li, lj, lk;
@@ -231,7 +269,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_pair_tile(TileArgs T) {
             if (a.start[c + 1] - a.start[c] > kCap) over = true;
         }
         if (__any_sync(0xffffffffu, over)) {
-            if (lane == 0) {
+            if (lane == 0 && grp == 0) {
                 const int k = atomicAdd(T.overflow_count, 1);
                 T.overflow_list[k] = home;
             }
@@ -240,8 +278,9 @@ __global__ void __launch_bounds__(kWarps * 32) k_pair_tile(TileArgs T) {
         stage<kDPD, kFlux, kSig>(a, S, D, 0, h0, nh, lane);
         __syncwarp();
 
-        // 14 tasks: offsets 13 (self) and 14..26 (the lexicographically positive ones)
-        for (int d = 13; d < 27; d++) {
+        // 14 tasks: offsets 13 (self) and 14..26 (the lexicographically positive ones);
+        // this work item runs tasks [13 + grp*per, 13 + (grp+1)*per)
+        for (int d = 13 + grp * per; d < 13 + (grp + 1) * per; d++) {
             const int ox = d / 9 - 1, oy = (d / 3) % 3 - 1, oz = d % 3 - 1;
             const bool self = (d == 13);
             int g0 = h0, nn = nh, base = 0;
@@ -287,16 +326,15 @@ __global__ void __launch_bounds__(kWarps * 32) k_pair_tile(TileArgs T) {
                 __syncwarp();
                 if (qtail - qhead >= 32) {
                     const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
-                    eval_pair<kDPD, kFlux, kDensity, kSig>(T, S, D, spots, blob, e & 0xffff, e >> 16, sh, epot, vir);
+                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, D, spots, blob, true, e, sh, lane, epot, vir);
                     qhead += 32;
                     __syncwarp();
                 }
             }
             if (qtail > qhead) {
-                if (lane < qtail - qhead) {
-                    const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
-                    eval_pair<kDPD, kFlux, kDensity, kSig>(T, S, D, spots, blob, e & 0xffff, e >> 16, sh, epot, vir);
-                }
+                const bool act = lane < qtail - qhead;
+                const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
+                eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, D, spots, blob, act, e, sh, lane, epot, vir);
             }
             __syncwarp();
             if (!self) {
@@ -465,7 +503,7 @@ void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
         if (per_sm < 1) per_sm = 1;
         occ_smem = smem;
     }
-    const int want = (T.a.P.ncells + kWarps - 1) / kWarps;
+    const int want = (T.a.P.ncells * T.split + kWarps - 1) / kWarps;
     const int grid = std::max(1, std::min(want, sms * per_sm));
     k_pair_tile<kDPD, kFlux, kDensity, kSig><<<grid, kWarps * 32, smem, s>>>(T);
     k_pair_overflow<kDPD, kFlux, kDensity, kSig><<<sms, 256, 0, s>>>(T);
@@ -476,11 +514,12 @@ void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
 int pair_tile_capacity() { return kCap; }
 
 void launch_pair_tile(const PairKernelArgs &a, int *overflow_list, int *overflow_count, int sms, bool signature,
-                      cudaStream_t s) {
+                      int split, cudaStream_t s) {
     TileArgs T;
     T.a = a;
     T.overflow_list = overflow_list;
     T.overflow_count = overflow_count;
+    T.split = (split == 1 || split == 2 || split == 7 || split == 14) ? split : 1;
     cudaMemsetAsync(overflow_count, 0, sizeof(int), s);
     if (a.n <= 0) return;
     const bool dpd = a.has_dpd, flux = a.P.nspec > 0 && a.has_flux;

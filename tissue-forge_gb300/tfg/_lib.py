@@ -49,6 +49,8 @@ def lib():
     L.tfg_force_only.argtypes = [E, C.c_int]
     L.tfg_sync.argtypes = [E]
     L.tfg_pair_signature.argtypes = [E, abi.I_P, abi.U_P]
+    L.tfg_autotune.argtypes = [E, C.POINTER(C.c_int)]
+    L.tfg_set_split.argtypes = [E, C.c_int]
     L.tfg_get_count.argtypes = [E, C.POINTER(C.c_int)]
     L.tfg_download.argtypes = [E, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P]
     L.tfg_get_reductions.argtypes = [E, C.POINTER(abi.Reductions)]

@@ -131,6 +131,15 @@ class Engine:
         self._chk(self.L.tfg_pair_signature(self.h, _ip(cnt), _up(hsh)), "pair_signature")
         return cnt, hsh
 
+    def autotune(self):
+        """Time the nonbonded pass's work splits on the current state; returns the chosen split."""
+        v = C.c_int()
+        self._chk(self.L.tfg_autotune(self.h, C.byref(v)), "autotune")
+        return v.value
+
+    def set_split(self, split):
+        self._chk(self.L.tfg_set_split(self.h, split), "set_split")
+
     def set_stream(self, stream_ptr):
         """Order the engine's work on the caller's CUDA stream (cudaStream_t as int)."""
         self._chk(self.L.tfg_engine_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
