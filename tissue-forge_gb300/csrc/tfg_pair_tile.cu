@@ -25,26 +25,19 @@ namespace tfg {
 namespace {
 
 constexpr int kWarps = 8;
-constexpr int kCap = 64;            // particles of one cell staged per warp (home and neighbour)
+constexpr int kCapT = 192;          // staged particles per warp: home cell + neighbour segments
+constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
 constexpr int kQ = 64;              // candidate ring queue entries per warp (power of two)
 constexpr int kMaxSmemTable = 4096; // floats of potential table staged per CTA
 
 struct Staged {
-    float4 pos[2 * kCap];   // [0,kCap): home, [kCap,2kCap): neighbour ; w = type bits
-    float4 acc[2 * kCap];   // fx, fy, fz, number density
-    float2 rid[2 * kCap];   // radius, id bits
-    uint32_t q[kQ];         // packed (i | j << 16), indices into the staged arrays
-};
-
-struct StagedDyn {         // DPD and flux extras
-    float4 vel[2 * kCap];
-    float sval[2 * kCap];  // species 0 (flux supports one species in the tiled path)
-    float sq[2 * kCap];
-};
-
-template <bool kDPD, bool kFlux> struct SmemLayout {
-    Staged st[kWarps];
-    StagedDyn dyn[(kDPD || kFlux) ? kWarps : 1];
+    float4 pos[kCapT];      // cell-relative position; w = type bits
+    float4 acc[kCapT];      // fx, fy, fz, number density (signature: count, hash bits)
+    int32_t gslot[kCapT];   // global slot of the staged particle
+    uint8_t seg[kCapT];     // task (stencil offset 13..26) of the staged particle's segment
+    float sh[27][3];        // shift of each task's partner cell (space_getsid)
+    uint32_t q[kQ];         // packed hit (i | k << 16), staged indices
+    float sq[kCapT];        // flux increment accumulators (species 0)
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -60,44 +53,38 @@ struct TileArgs {
     int split;             // warps per home cell: the 14 tasks are divided into `split` groups
 };
 
-// Evaluate one interacting pair (reference orientation: I = part_i, J = part_j) and
-// accumulate into the staged accumulators of both.
-template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
-__device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, StagedDyn &D, const PotDev *pots,
-                                          const float *blob, int I, int J, float3 sh, float &epot, float &vir,
-                                          float4 &fI) {
+// Evaluate one interacting pair, reference orientation I = part_i (home), K = part_j.
+// Returns the I-side and K-side increments (force xyz, density) in fI / fK.
+template <bool kDPD, bool kFlux, bool kDensity>
+__device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, const PotDev *pots, const float *blob, int I,
+                                          int K, float &epot, float &vir, float4 &fI, float4 &fK) {
     const PairKernelArgs &a = T.a;
     const SimParams &P = a.P;
-    const float4 pi = S.pos[I], pj = S.pos[J];
+    const float4 pi = S.pos[I], pk = S.pos[K];
+    const int sg = S.seg[K];
+    const float3 sh = make_float3(S.sh[sg][0], S.sh[sg][1], S.sh[sg][2]);
     float3 dx;
-    const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z), sh, make_float3(pj.x, pj.y, pj.z), dx);
-    if (kSig) {
-        // counters live in the accumulator bits: x = count, y = hash (integer atomics)
-        atomicAdd(reinterpret_cast<int *>(&S.acc[I].x), 1);
-        atomicAdd(reinterpret_cast<int *>(&S.acc[J].x), 1);
-        atomicAdd(reinterpret_cast<unsigned *>(&S.acc[I].y), sig_mix((uint32_t)__float_as_int(S.rid[J].y)));
-        atomicAdd(reinterpret_cast<unsigned *>(&S.acc[J].y), sig_mix((uint32_t)__float_as_int(S.rid[I].y)));
-        return;
-    }
+    const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z), sh, make_float3(pk.x, pk.y, pk.z), dx);
     const float r = __fsqrt_rn(r2);
     if (kDensity) {
         const float w = density_w(r, 1.0f / P.cutoff, P.self_density);
         fI.w += w;
-        atomicAdd(&S.acc[J].w, w);
+        fK.w += w;
     }
-    const int ti = __float_as_int(pi.w), tj = __float_as_int(pj.w);
-    const int pidx = ti * P.max_type + tj;
+    const int ti = __float_as_int(pi.w), tk = __float_as_int(pk.w);
+    const int pidx = ti * P.max_type + tk;
+    const int gi = S.gslot[I], gk = S.gslot[K];
     if (kFlux) {
         const FluxSet &fs = a.fluxes[pidx];
-        for (int k = 0; k < fs.count; k++) {
-            const FluxDev &F = fs.f[k];
+        for (int f = 0; f < fs.count; f++) {
+            const FluxDev &F = fs.f[f];
             if (r > F.cutoff) continue;
             float term = __fsub_rn(1.0f, __fdiv_rn(r, F.cutoff));
             term = __fmul_rn(term, term);
             const bool a_is_I = (ti == F.type_a);
-            const bool b_is_J = (tj == F.type_b);
-            const int sa = a_is_I ? I : J, sb = b_is_J ? J : I;
-            const float ssi = D.sval[sa], ssj = D.sval[sb];
+            const bool b_is_K = (tk == F.type_b);
+            const int sa = a_is_I ? I : K, sb = b_is_K ? K : I;
+            const float ssi = a.sval[a_is_I ? gi : gk], ssj = a.sval[b_is_K ? gk : gi];
             float q = term;
             if (F.kind == TFG_FLUX_FICK) {
                 q = __fmul_rn(q, __fmul_rn(F.coef, __fsub_rn(ssi, ssj)));
@@ -108,66 +95,71 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, StagedDy
                 const float qq = __fmul_rn(__fmul_rn(F.coef, __fsub_rn(F.target, ssj)), ssi);
                 q = __fmul_rn(q, qq > 0.f ? qq : 0.f);
             }
-            atomicAdd(&D.sq[sa], -q - F.half_decay * ssi);
-            atomicAdd(&D.sq[sb], q - F.half_decay * ssj);
+            atomicAdd(&S.sq[sa], -q - F.half_decay * ssi);
+            atomicAdd(&S.sq[sb], q - F.half_decay * ssj);
         }
     }
     const PotDev &pot = pots[pidx];
     if (pot.kind == POT_TABLE) {
         float e, f;
-        if (table_eval(pot, blob, S.rid[I].x, S.rid[J].x, r2, e, f)) {
+        const float ri = a.aux[gi].x, rk = a.aux[gk].x;
+        if (table_eval(pot, blob, ri, rk, r2, e, f)) {
             const float wx = f * dx.x, wy = f * dx.y, wz = f * dx.z;
-            fI.x -= wx;
-            fI.y -= wy;
-            fI.z -= wz;
-            atomicAdd(&S.acc[J].x, wx);
-            atomicAdd(&S.acc[J].y, wy);
-            atomicAdd(&S.acc[J].z, wz);
+            fI.x -= wx; fI.y -= wy; fI.z -= wz;
+            fK.x += wx; fK.y += wy; fK.z += wz;
             epot += e;
             vir -= f * r2;
         }
     } else if (kDPD && pot.kind == POT_DPD) {
+        const float4 axi = a.aux[gi], axk = a.aux[gk];
         float rr = r;
         const float ro = r < 1.1920928955078125e-7f ? 1.1920928955078125e-7f : r;
-        if (pot.flags & TFG_POTENTIAL_SHIFTED) rr = __fsub_rn(rr, __fadd_rn(S.rid[I].x, S.rid[J].x));
+        if (pot.flags & TFG_POTENTIAL_SHIFTED) rr = __fsub_rn(rr, __fadd_rn(axi.x, axk.x));
         if (rr <= pot.b) {
             rr = rr >= pot.a ? rr : pot.a;
-            const float4 vi = D.vel[I], vj = D.vel[J];
+            const float4 vi = a.vel[gi], vk = a.vel[gk];
             const float inv_ro = 1.0f / ro;
             const float ex = dx.x * inv_ro, ey = dx.y * inv_ro, ez = dx.z * inv_ro;
             const float omega_c = rr < 0.f ? 1.f : 1.f - rr / pot.b;
-            const float edv = ex * (vi.x - vj.x) + ey * (vi.y - vj.y) + ez * (vi.z - vj.z);
+            const float edv = ex * (vi.x - vk.x) + ey * (vi.y - vk.y) + ez * (vi.z - vk.z);
             float xi_r = 1.0f;
             if (!(P.flags & TFG_ENGINE_DPD_REFERENCE_RANDOM))
-                xi_r = gauss_pair(P.seed, P.time, __float_as_int(S.rid[I].y), __float_as_int(S.rid[J].y));
+                xi_r = gauss_pair(P.seed, P.time, __float_as_int(axi.w), __float_as_int(axk.w));
             const float ftot = pot.dpd_alpha * omega_c - pot.dpd_gamma * omega_c * omega_c * edv +
                                pot.dpd_sigma * omega_c * xi_r * P.dpd_delta;
             const float wx = ftot * ex, wy = ftot * ey, wz = ftot * ez;
             // part_i.f += F e ; part_j.f -= F e
-            fI.x += wx;
-            fI.y += wy;
-            fI.z += wz;
-            atomicAdd(&S.acc[J].x, -wx);
-            atomicAdd(&S.acc[J].y, -wy);
-            atomicAdd(&S.acc[J].z, -wz);
+            fI.x += wx; fI.y += wy; fI.z += wz;
+            fK.x -= wx; fK.y -= wy; fK.z -= wz;
             vir += ftot * ro;
         }
     }
 }
 
-// Evaluate the queued pairs held by the active lanes (entries in enumeration order, so
-// equal I form contiguous runs).  The I side is reduced over each run with a segmented
-// warp scan and written once per distinct I by the run's last lane; the J side (rarely
-// repeated inside a batch) uses shared-memory atomics.
+// Evaluate the queued hits held by the active lanes.  Entries are in enumeration order
+// (i-major), so equal I form contiguous runs: the I side is summed by a segmented warp
+// scan and written by each run's last lane.  Equal K are grouped with match_any and
+// summed into the group's lowest lane.  Every accumulator write is then unique within
+// the batch, so plain shared-memory read-modify-writes suffice.
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
-__device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, StagedDyn &D, const PotDev *pots,
-                                           const float *blob, bool active, uint32_t e, float3 sh, int lane,
-                                           float &epot, float &vir) {
-    const int I = e & 0xffff, J = e >> 16;
-    float4 fI = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (active) eval_pair<kDPD, kFlux, kDensity, kSig>(T, S, D, pots, blob, I, J, sh, epot, vir, fI);
-    if (kSig) return;
-    const int key = active ? I : 1024 + lane;
+__device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, const PotDev *pots, const float *blob,
+                                           bool active, uint32_t e, int lane, float &epot, float &vir) {
+    const int I = e & 0xffff, K = e >> 16;
+    if (kSig) {
+        if (active) {
+            atomicAdd(reinterpret_cast<int *>(&S.acc[I].x), 1);
+            atomicAdd(reinterpret_cast<int *>(&S.acc[K].x), 1);
+            const uint32_t idi = (uint32_t)__float_as_int(T.a.aux[S.gslot[I]].w);
+            const uint32_t idk = (uint32_t)__float_as_int(T.a.aux[S.gslot[K]].w);
+            atomicAdd(reinterpret_cast<unsigned *>(&S.acc[I].y), sig_mix(idk));
+            atomicAdd(reinterpret_cast<unsigned *>(&S.acc[K].y), sig_mix(idi));
+        }
+        return;
+    }
+    float4 fI = make_float4(0.f, 0.f, 0.f, 0.f), fK = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (active) eval_pair<kDPD, kFlux, kDensity>(T, S, pots, blob, I, K, epot, vir, fI, fK);
+    // I side: segmented inclusive scan over contiguous runs
+    const int key = active ? I : 4096 + lane;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const int k2 = __shfl_up_sync(0xffffffffu, key, o);
@@ -180,64 +172,79 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, StagedD
         }
     }
     const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+    // K side: groups of equal K, summed into the lowest lane of each group
+    const int kkey = active ? K : 8192 + lane;
+    const uint32_t grp = __match_any_sync(0xffffffffu, kkey);
+    const uint32_t others = grp & ~(1u << lane);
+    const int rounds = __reduce_max_sync(0xffffffffu, (uint32_t)__popc(others));
+    const bool leader = (grp & lanemask_lt()) == 0;
+    uint32_t rest = others;
+    for (int r = 0; r < rounds; r++) {
+        const int src = rest ? __ffs(rest) - 1 : lane;
+        rest &= rest - 1;
+        const float x = __shfl_sync(0xffffffffu, fK.x, src);
+        const float y = __shfl_sync(0xffffffffu, fK.y, src);
+        const float z = __shfl_sync(0xffffffffu, fK.z, src);
+        const float w = __shfl_sync(0xffffffffu, fK.w, src);
+        if (leader && src != lane) {
+            fK.x += x; fK.y += y; fK.z += z; fK.w += w;
+        }
+    }
     if (active && (lane == 31 || knext != key)) {
         float4 v = S.acc[I];
         v.x += fI.x; v.y += fI.y; v.z += fI.z; v.w += fI.w;
         S.acc[I] = v;
     }
-}
-
-// Stage `n` particles of global slots [g0, g0+n) into staged index base..base+n.
-template <bool kDPD, bool kFlux, bool kSig>
-__device__ __forceinline__ void stage(const PairKernelArgs &a, Staged &S, StagedDyn &D, int base, int g0, int n,
-                                      int lane) {
-    for (int k = lane; k < n; k += 32) {
-        const int g = g0 + k;
-        S.pos[base + k] = a.pos[g];
-        const float4 ax = a.aux[g];
-        S.rid[base + k] = make_float2(ax.x, ax.w);
-        S.acc[base + k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (!kSig && kDPD) D.vel[base + k] = a.vel[g];
-        if (!kSig && kFlux) {
-            D.sval[base + k] = a.sval[g];
-            D.sq[base + k] = 0.f;
-        }
+    __syncwarp();
+    if (active && leader) {
+        float4 v = S.acc[K];
+        v.x += fK.x; v.y += fK.y; v.z += fK.z; v.w += fK.w;
+        S.acc[K] = v;
     }
 }
 
-// Flush staged accumulators of [base, base+n) to the particles at global slots g0...
 template <bool kFlux, bool kSig>
-__device__ __forceinline__ void flush(const PairKernelArgs &a, Staged &S, StagedDyn &D, int base, int g0, int n,
+__device__ __forceinline__ void stage(const PairKernelArgs &a, Staged &S, int base, int g0, int n, int task,
                                       int lane) {
     for (int k = lane; k < n; k += 32) {
-        const float4 v = S.acc[base + k];
+        S.pos[base + k] = a.pos[g0 + k];
+        S.acc[base + k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        S.gslot[base + k] = g0 + k;
+        S.seg[base + k] = (uint8_t)task;
+        if (!kSig && kFlux) S.sq[base + k] = 0.f;
+    }
+}
+
+template <bool kFlux, bool kSig>
+__device__ __forceinline__ void flush(const PairKernelArgs &a, Staged &S, int b0, int b1, int lane) {
+    for (int k = b0 + lane; k < b1; k += 32) {
+        const float4 v = S.acc[k];
+        const int g = S.gslot[k];
         if (kSig) {
-            const int id = __float_as_int(S.rid[base + k].y);
             const int c = __float_as_int(v.x);
             if (c) {
+                const int id = __float_as_int(a.aux[g].w);
                 atomicAdd(&a.sig_count[id], c);
                 atomicAdd(&a.sig_hash[id], (uint32_t)__float_as_int(v.y));
             }
             continue;
         }
-        if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(&a.force[g0 + k], v);
+        if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(&a.force[g], v);
         if (kFlux) {
-            const float q = D.sq[base + k];
-            if (q != 0.f) atomicAdd(&a.sq[g0 + k], q);
+            const float q = S.sq[k];
+            if (q != 0.f) atomicAdd(&a.sq[g], q);
         }
     }
 }
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
-__global__ void __launch_bounds__(kWarps * 32) k_pair_tile(TileArgs T) {
+__global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    using Layout = SmemLayout<kDPD, kFlux>;
-    Layout &L = *reinterpret_cast<Layout *>(smem_raw);
-    float *sblob = reinterpret_cast<float *>(smem_raw + sizeof(Layout));
+    Staged *L = reinterpret_cast<Staged *>(smem_raw);
+    float *sblob = reinterpret_cast<float *>(smem_raw + sizeof(Staged) * kWarps);
     const PairKernelArgs &a = T.a;
     const SimParams &P = a.P;
 
-    // potential tables and descriptors, shared by the CTA
     const int nb = a.blob_floats <= kMaxSmemTable ? a.blob_floats : 0;
     for (int k = threadIdx.x; k < nb; k += blockDim.x) sblob[k] = a.blob[k];
     PotDev *spots = reinterpret_cast<PotDev *>(sblob + ((nb + 3) & ~3));
@@ -247,27 +254,37 @@ __global__ void __launch_bounds__(kWarps * 32) k_pair_tile(TileArgs T) {
     const float *blob = nb ? sblob : a.blob;
 
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    Staged &S = L.st[wid];
-    StagedDyn &D = L.dyn[(kDPD || kFlux) ? wid : 0];
+    Staged &S = L[wid];
     float epot = 0.f, vir = 0.f;
     const int nwarps_total = gridDim.x * kWarps;
-
-    const int per = 14 / T.split;                       // tasks per work item
+    const int per = 14 / T.split;
     const int nitems = P.ncells * T.split;
+
     for (int item = blockIdx.x * kWarps + wid; item < nitems; item += nwarps_total) {
         const int home = item / T.split, grp = item - home * T.split;
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         if (nh == 0) continue;
+        const int t0 = 13 + grp * per, t1 = t0 + per;
         int li, lj, lk;
         cell_loc(P, home, li, lj, lk);
-        // capacity check over the home cell and its forward neighbours
-        bool over = nh > kCap;
-        for (int d = 14 + lane; d < 27 && !over; d += 32) {
+        // lane L (< 13) describes forward task 14+L: partner cell start, count and shift
+        int my_g0 = 0, my_n = 0;
+        if (lane < 13) {
+            const int d = 14 + lane;
             const int ox = d / 9 - 1, oy = (d / 3) % 3 - 1, oz = d % 3 - 1;
-            const int c = cell_index(P, (li + ox + P.cdim[0]) % P.cdim[0], (lj + oy + P.cdim[1]) % P.cdim[1],
-                                     (lk + oz + P.cdim[2]) % P.cdim[2]);
-            if (a.start[c + 1] - a.start[c] > kCap) over = true;
+            const int mi = (li + ox + P.cdim[0]) % P.cdim[0];
+            const int mj = (lj + oy + P.cdim[1]) % P.cdim[1];
+            const int mk = (lk + oz + P.cdim[2]) % P.cdim[2];
+            const int c = cell_index(P, mi, mj, mk);
+            my_g0 = a.start[c];
+            my_n = a.start[c + 1] - my_g0;
+            S.sh[d][0] = cell_shift(P, 0, li, mi);
+            S.sh[d][1] = cell_shift(P, 1, lj, mj);
+            S.sh[d][2] = cell_shift(P, 2, lk, mk);
         }
+        if (lane == 13) { S.sh[13][0] = 0.f; S.sh[13][1] = 0.f; S.sh[13][2] = 0.f; }
+        // capacity: every group of this home cell takes the same decision
+        const bool over = nh > kHomeCap || (lane < 13 && nh + my_n > kCapT);
         if (__any_sync(0xffffffffu, over)) {
             if (lane == 0 && grp == 0) {
                 const int k = atomicAdd(T.overflow_count, 1);
@@ -275,74 +292,69 @@ __global__ void __launch_bounds__(kWarps * 32) k_pair_tile(TileArgs T) {
             }
             continue;
         }
-        stage<kDPD, kFlux, kSig>(a, S, D, 0, h0, nh, lane);
+        stage<kFlux, kSig>(a, S, 0, h0, nh, 13, lane);
         __syncwarp();
 
-        // 14 tasks: offsets 13 (self) and 14..26 (the lexicographically positive ones);
-        // this work item runs tasks [13 + grp*per, 13 + (grp+1)*per)
-        for (int d = 13 + grp * per; d < 13 + (grp + 1) * per; d++) {
-            const int ox = d / 9 - 1, oy = (d / 3) % 3 - 1, oz = d % 3 - 1;
-            const bool self = (d == 13);
-            int g0 = h0, nn = nh, base = 0;
-            float3 sh = make_float3(0.f, 0.f, 0.f);
-            if (!self) {
-                const int mi = (li + ox + P.cdim[0]) % P.cdim[0];
-                const int mj = (lj + oy + P.cdim[1]) % P.cdim[1];
-                const int mk = (lk + oz + P.cdim[2]) % P.cdim[2];
-                const int c = cell_index(P, mi, mj, mk);
-                g0 = a.start[c];
-                nn = a.start[c + 1] - g0;
-                if (nn == 0) continue;
-                base = kCap;
-                sh.x = cell_shift(P, 0, li, mi);
-                sh.y = cell_shift(P, 1, lj, mj);
-                sh.z = cell_shift(P, 2, lk, mk);
-                stage<kDPD, kFlux, kSig>(a, S, D, kCap, g0, nn, lane);
-                __syncwarp();
-            } else if (nh < 2) {
-                continue;
-            }
-            // candidates (i in home, j in partner); self: i < j
-            const int total = nh * nn;
-            const float inv_nn = 1.0f / (float)nn;
-            int qhead = 0, qtail = 0;   // warp-uniform ring indices
-            for (int p0 = 0; p0 < total; p0 += 32) {
-                const int p = p0 + lane;
-                bool hit = false;
-                int i = 0, j = 0;
-                if (p < total) {
-                    i = (int)(((float)p + 0.5f) * inv_nn);
-                    j = p - i * nn;
-                    if (!self || i < j) {
-                        float3 dx;
-                        const float4 pi = S.pos[i], pj = S.pos[base + j];
-                        const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z), sh, make_float3(pj.x, pj.y, pj.z), dx);
-                        hit = r2 <= P.cutoff2;
-                    }
-                }
-                const uint32_t m = __ballot_sync(0xffffffffu, hit);
-                if (hit) S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)(base + j) << 16);
-                qtail += __popc(m);
-                __syncwarp();
-                if (qtail - qhead >= 32) {
-                    const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
-                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, D, spots, blob, true, e, sh, lane, epot, vir);
-                    qhead += 32;
-                    __syncwarp();
-                }
-            }
-            if (qtail > qhead) {
-                const bool act = lane < qtail - qhead;
-                const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
-                eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, D, spots, blob, act, e, sh, lane, epot, vir);
+        int t = t0 < 14 ? 14 : t0;     // next neighbour task to stage
+        bool with_self = (t0 == 13);
+        while (with_self || t < t1) {
+            // stage as many neighbour segments as fit after the home cell
+            int end = nh;
+            while (t < t1) {
+                const int g0 = __shfl_sync(0xffffffffu, my_g0, t - 14);
+                const int nn = __shfl_sync(0xffffffffu, my_n, t - 14);
+                if (end + nn > kCapT) break;
+                if (nn > 0) stage<kFlux, kSig>(a, S, end, g0, nn, t, lane);
+                end += nn;
+                t++;
             }
             __syncwarp();
-            if (!self) {
-                flush<kFlux, kSig>(a, S, D, kCap, g0, nn, lane);
+            const int tbeg = with_self ? 0 : nh;
+            const int ntgt = end - tbeg;
+            with_self = false;
+            const int total = nh * ntgt;
+            int qhead = 0, qtail = 0;
+            if (total > 0) {
+                const float inv_nt = 1.0f / (float)ntgt;
+                for (int p0 = 0; p0 < total; p0 += 32) {
+                    const int p = p0 + lane;
+                    bool hit = false;
+                    int i = 0, k = 0;
+                    if (p < total) {
+                        i = (int)(((float)p + 0.5f) * inv_nt);
+                        k = tbeg + (p - i * ntgt);
+                        if (k >= nh || i < k) {
+                            const int sg = S.seg[k];
+                            const float4 pi = S.pos[i], pk = S.pos[k];
+                            float3 dx;
+                            const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z),
+                                                     make_float3(S.sh[sg][0], S.sh[sg][1], S.sh[sg][2]),
+                                                     make_float3(pk.x, pk.y, pk.z), dx);
+                            hit = r2 <= P.cutoff2;
+                        }
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, hit);
+                    if (hit) S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)k << 16);
+                    qtail += __popc(m);
+                    __syncwarp();
+                    if (qtail - qhead >= 32) {
+                        const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
+                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, spots, blob, true, e, lane, epot, vir);
+                        qhead += 32;
+                        __syncwarp();
+                    }
+                }
+                if (qtail > qhead) {
+                    const bool act = lane < qtail - qhead;
+                    const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
+                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, spots, blob, act, e, lane, epot, vir);
+                }
                 __syncwarp();
             }
+            flush<kFlux, kSig>(a, S, nh, end, lane);
+            __syncwarp();
         }
-        flush<kFlux, kSig>(a, S, D, 0, h0, nh, lane);
+        flush<kFlux, kSig>(a, S, 0, nh, lane);
         __syncwarp();
     }
     if (kSig) return;
@@ -484,11 +496,10 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
 void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
-    using Layout = SmemLayout<kDPD, kFlux>;
-    const size_t smem_max = sizeof(Layout) + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxTypes * kMaxTypes;
+    const size_t base = sizeof(Staged) * kWarps;
+    const size_t smem_max = base + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxTypes * kMaxTypes;
     const int nb = T.a.blob_floats <= kMaxSmemTable ? T.a.blob_floats : 0;
-    const size_t smem = sizeof(Layout) + sizeof(float) * ((nb + 3) & ~3) +
-                        sizeof(PotDev) * T.a.P.max_type * T.a.P.max_type;
+    const size_t smem = base + sizeof(float) * ((nb + 3) & ~3) + sizeof(PotDev) * T.a.P.max_type * T.a.P.max_type;
     static bool configured = false;
     static size_t occ_smem = 0;
     static int per_sm = 1;
@@ -511,7 +522,7 @@ void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
 
 }  // namespace
 
-int pair_tile_capacity() { return kCap; }
+int pair_tile_capacity() { return kCapT; }
 
 void launch_pair_tile(const PairKernelArgs &a, int *overflow_list, int *overflow_count, int sms, bool signature,
                       int split, cudaStream_t s) {
