@@ -51,13 +51,22 @@ FLOPS = dict(table=50, dpd=45, flux=12, density=12, bond=45, angle=75, integrate
              integrate_overdamped=15)
 
 
-def make_workload(name, seed):
+def make_workload(name, seed, n=None, relax=None):
+    """The named workload at its configured size, or scaled to n particles (same density)."""
     from tfg import configs
     if name == "dpd_droplets":
+        if n:
+            scale = (n / 100_000) ** (1.0 / 3.0)
+            return configs.dpd_droplets(n=n, side=40.0 * scale, radius=12.0 * scale, seed=1 + seed)
         return configs.dpd_droplets(seed=1 + seed)
     if name == "bonded_fluid":
-        return configs.bonded_fluid(seed=2 + seed)
+        w = configs.bonded_fluid(n=n or 2_000_000, seed=2 + seed)
+        if relax is not None:
+            w.relax_steps = relax
+        return w
     if name == "cell_sorting":
+        if n:
+            return configs.cell_sorting(n=n, side=20.0 * (n / 4000) ** (1.0 / 3.0), seed=seed)
         return configs.cell_sorting(seed=seed)
     raise SystemExit("unknown workload " + name)
 
@@ -149,7 +158,7 @@ def cpu_reference_rate(w, threads, budget_s, max_steps=200):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    w = make_workload(args.workload, 0)
+    w = make_workload(args.workload, 0, args.n or None, args.relax)
     threads = os.cpu_count() or 1
     budget = 20.0
     rates = []
@@ -183,6 +192,8 @@ def main():
     ap.add_argument("--impl", default="tfg", choices=["tfg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--n", type=int, default=0, help="scale the workload to n particles (same density)")
+    ap.add_argument("--relax", type=int, default=None, help="override the relaxation steps")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -214,7 +225,7 @@ def main():
     from tfg import lib
     from tfg.engine import Engine, setup_model
 
-    w = make_workload(args.workload, rank)
+    w = make_workload(args.workload, rank, args.n or None, args.relax)
     eng = Engine(w.desc(device=dev))
     keep = setup_model(eng, w)
     # a dedicated (non-default) stream shared by the engine and the timing events
