@@ -228,13 +228,24 @@ __global__ void k_place(int n, const int32_t *cell, const int32_t *lidx, const i
     tmp_src[p] = i;
 }
 
-// Deterministic order inside a cell: rank by particle id (one warp per cell).
+// Deterministic order inside a cell: rank by particle id (one warp per cell).  Cells of
+// up to 32 particles rank in registers (one id per lane, compared through shuffles);
+// larger cells compare against global memory.
 __global__ void k_rank(int ncells, const int32_t *start, const int32_t *tmp_id, const int32_t *tmp_src,
                        int32_t *dest) {
     int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (w >= ncells) return;
     int s0 = start[w], s1 = start[w + 1];
+    const int n = s1 - s0;
+    if (n == 0) return;
+    if (n <= 32) {
+        const int my = lane < n ? tmp_id[s0 + lane] : 0x7fffffff;
+        int r = 0;
+        for (int o = 0; o < n; o++) r += __shfl_sync(0xffffffffu, my, o) < my;
+        if (lane < n) dest[tmp_src[s0 + lane]] = s0 + r;
+        return;
+    }
     for (int e = s0 + lane; e < s1; e += 32) {
         int my = tmp_id[e];
         int r = 0;
@@ -290,9 +301,21 @@ __global__ void k_scatter(int n, int cap, int nspec, const int32_t *dest, Partic
 
 __device__ __forceinline__ int wrap_shift(int s) { return s > 1 ? -1 : (s < -1 ? 1 : s); }
 
-__device__ __forceinline__ void warp_add_double(double *dst, double v) {
+// Block reduction of a per-thread FP32 partial into an FP64 global total: FP32 sums over
+// each warp, FP64 across the warps of the block, one FP64 atomic per block.  Every
+// thread of the block must call it (it synchronises the block).
+__device__ __forceinline__ void block_add(double *dst, float v) {
+    __shared__ double part[32];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(dst, v);
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) part[w] = (double)v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < nw; k++) t += part[k];
+        if (t != 0.0) atomicAdd(dst, t);
+    }
 }
 
 // bond_eval (tfBond.cpp:97-345) for table potentials; one thread per bond.
@@ -300,7 +323,7 @@ __global__ void k_bonds(int nb, SimParams P, const int2 *bonds, const int32_t *b
                         const float *bblob, const int32_t *slot_of_id, const float4 *pos, const float4 *aux,
                         const int32_t *cell, float4 *force, double *red) {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
-    double epot = 0.0, vir = 0.0;
+    float epot = 0.f, vir = 0.f;
     if (b < nb) {
         int2 bd = bonds[b];
         const PotDev &pot = bpots[bslot[b]];
@@ -338,19 +361,15 @@ __global__ void k_bonds(int nb, SimParams P, const int2 *bonds, const int32_t *b
                     ee = fmaf(ee, x, c[k]);
                 }
                 float f = eff * c[1] / rb;
-                atomicAdd(&force[si].x, -f * dx);
-                atomicAdd(&force[si].y, -f * dy);
-                atomicAdd(&force[si].z, -f * dz);
-                atomicAdd(&force[sj].x, f * dx);
-                atomicAdd(&force[sj].y, f * dy);
-                atomicAdd(&force[sj].z, f * dz);
+                atomicAdd(&force[si], make_float4(-f * dx, -f * dy, -f * dz, 0.f));
+                atomicAdd(&force[sj], make_float4(f * dx, f * dy, f * dz, 0.f));
                 epot = ee;
-                vir = -(double)f * (double)r2;
+                vir = -f * r2;
             }
         }
     }
-    warp_add_double(&red[RED_EPOT_BOND], epot);
-    warp_add_double(&red[RED_VIRIAL], vir);
+    block_add(&red[RED_EPOT_BOND], epot);
+    block_add(&red[RED_VIRIAL], vir);
 }
 
 // angle_eval (tfAngle.cpp:90-382); one thread per angle, j is the vertex.
@@ -358,7 +377,7 @@ __global__ void k_angles(int na, SimParams P, const int4 *angles, const PotDev *
                          const int32_t *slot_of_id, const float4 *pos, const int32_t *cell, float4 *force,
                          double *red) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
-    double epot = 0.0;
+    float epot = 0.f;
     if (q < na) {
         int4 A = angles[q];
         const PotDev &pot = bpots[A.w];
@@ -420,21 +439,15 @@ __global__ void k_angles(int na, SimParams P, const int4 *angles, const PotDev *
                     eff = eff * c[1];
                     float wi[3], wk[3];
                     for (int k = 0; k < 3; k++) { wi[k] = eff * dxi[k]; wk[k] = eff * dxk[k]; }
-                    atomicAdd(&force[si].x, -wi[0]);
-                    atomicAdd(&force[si].y, -wi[1]);
-                    atomicAdd(&force[si].z, -wi[2]);
-                    atomicAdd(&force[sk].x, -wk[0]);
-                    atomicAdd(&force[sk].y, -wk[1]);
-                    atomicAdd(&force[sk].z, -wk[2]);
-                    atomicAdd(&force[sj].x, wi[0] + wk[0]);
-                    atomicAdd(&force[sj].y, wi[1] + wk[1]);
-                    atomicAdd(&force[sj].z, wi[2] + wk[2]);
+                    atomicAdd(&force[si], make_float4(-wi[0], -wi[1], -wi[2], 0.f));
+                    atomicAdd(&force[sk], make_float4(-wk[0], -wk[1], -wk[2], 0.f));
+                    atomicAdd(&force[sj], make_float4(wi[0] + wk[0], wi[1] + wk[1], wi[2] + wk[2], 0.f));
                     epot = ee;
                 }
             }
         }
     }
-    warp_add_double(&red[RED_EPOT_ANGLE], epot);
+    block_add(&red[RED_EPOT_ANGLE], epot);
 }
 
 // cell_advance_forward_euler + Fluxes_integrate; one thread per particle.
@@ -442,10 +455,10 @@ __global__ void k_advance(int n, int cap, SimParams P, float4 *pos, float4 *vel,
                           const float4 *force, int32_t *cell, float *sval, float *sq, const float *type_mass,
                           const int32_t *type_dyn, const uint32_t *species_flags, double *red, uint32_t *err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double ke = 0.0, vol = 0.0, mig = 0.0;
-    double stot[kMaxSpecies];
+    float ke = 0.f, vol = 0.f, mig = 0.f;
+    float stot[kMaxSpecies];
 #pragma unroll
-    for (int s = 0; s < kMaxSpecies; s++) stot[s] = 0.0;
+    for (int s = 0; s < kMaxSpecies; s++) stot[s] = 0.f;
     if (i < n) {
         float4 p = pos[i], v = vel[i];
         const float4 ax = aux[i];
@@ -453,8 +466,7 @@ __global__ void k_advance(int n, int cap, SimParams P, float4 *pos, float4 *vel,
         const int type = __float_as_int(p.w);
         const uint32_t flags = (uint32_t)__float_as_int(ax.z);
         const float imass = ax.y;
-        ke = 0.5 * (double)type_mass[type] *
-             ((double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z);
+        ke = 0.5f * type_mass[type] * (v.x * v.x + v.y * v.y + v.z * v.z);
         bool migrated = false;
         const bool frozen_all = (flags & TFG_PARTICLE_FROZEN_X) && (flags & TFG_PARTICLE_FROZEN_Y) &&
                                 (flags & TFG_PARTICLE_FROZEN_Z);
@@ -496,7 +508,7 @@ __global__ void k_advance(int n, int cap, SimParams P, float4 *pos, float4 *vel,
                 cell[i] = cell_index(P, (a + delta[0] + P.cdim[0]) % P.cdim[0], (b + delta[1] + P.cdim[1]) % P.cdim[1],
                                      (c + delta[2] + P.cdim[2]) % P.cdim[2]);
                 migrated = true;
-                mig = 1.0;
+                mig = 1.f;
             }
             if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) atomicOr(err, ERR_NAN);
             pos[i] = make_float4(x[0], x[1], x[2], p.w);
@@ -516,10 +528,10 @@ __global__ void k_advance(int n, int cap, SimParams P, float4 *pos, float4 *vel,
             stot[s] = sv;
         }
     }
-    warp_add_double(&red[RED_KINETIC], ke);
-    warp_add_double(&red[RED_VOLUME], vol);
-    warp_add_double(&red[RED_MIGRATIONS], mig);
-    for (int s = 0; s < P.nspec; s++) warp_add_double(&red[RED_SPECIES0 + s], stot[s]);
+    block_add(&red[RED_KINETIC], ke);
+    block_add(&red[RED_VOLUME], vol);
+    block_add(&red[RED_MIGRATIONS], mig);
+    for (int s = 0; s < P.nspec; s++) block_add(&red[RED_SPECIES0 + s], stot[s]);
 }
 
 __global__ void k_gather(int n, int cap, int nspec, SimParams P, ParticleArrays A, const float4 *force, float *x,

@@ -24,7 +24,7 @@ namespace tfg {
 
 namespace {
 
-constexpr int kWarps = 8;
+constexpr int kWarps = 4;
 constexpr int kCapT = 192;          // staged particles per warp: home cell + neighbour segments
 constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
 constexpr int kQ = 64;              // candidate ring queue entries per warp (power of two)
@@ -34,7 +34,7 @@ struct Staged {
     float4 pos[kCapT];      // cell-relative position; w = type bits
     float4 acc[kCapT];      // fx, fy, fz, number density (signature: count, hash bits)
     int32_t gslot[kCapT];   // global slot of the staged particle
-    uint8_t seg[kCapT];     // task (stencil offset 13..26) of the staged particle's segment
+    float4 sh4[kCapT];      // shift of the staged particle's cell as seen from the home cell
     float sh[27][3];        // shift of each task's partner cell (space_getsid)
     uint32_t q[kQ];         // packed hit (i | k << 16), staged indices
     float sq[kCapT];        // flux increment accumulators (species 0)
@@ -61,8 +61,8 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, const Po
     const PairKernelArgs &a = T.a;
     const SimParams &P = a.P;
     const float4 pi = S.pos[I], pk = S.pos[K];
-    const int sg = S.seg[K];
-    const float3 sh = make_float3(S.sh[sg][0], S.sh[sg][1], S.sh[sg][2]);
+    const float4 s4 = S.sh4[K];
+    const float3 sh = make_float3(s4.x, s4.y, s4.z);
     float3 dx;
     const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z), sh, make_float3(pk.x, pk.y, pk.z), dx);
     const float r = __fsqrt_rn(r2);
@@ -102,7 +102,11 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, const Po
     const PotDev &pot = pots[pidx];
     if (pot.kind == POT_TABLE) {
         float e, f;
-        const float ri = a.aux[gi].x, rk = a.aux[gk].x;
+        float ri = 0.f, rk = 0.f;
+        if (pot.flags & (TFG_POTENTIAL_SHIFTED | TFG_POTENTIAL_SCALED)) {
+            ri = a.aux[gi].x;
+            rk = a.aux[gk].x;
+        }
         if (table_eval(pot, blob, ri, rk, r2, e, f)) {
             const float wx = f * dx.x, wy = f * dx.y, wz = f * dx.z;
             fI.x -= wx; fI.y -= wy; fI.z -= wz;
@@ -206,11 +210,12 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, const P
 template <bool kFlux, bool kSig>
 __device__ __forceinline__ void stage(const PairKernelArgs &a, Staged &S, int base, int g0, int n, int task,
                                       int lane) {
+    const float4 sh = make_float4(S.sh[task][0], S.sh[task][1], S.sh[task][2], 0.f);
     for (int k = lane; k < n; k += 32) {
         S.pos[base + k] = a.pos[g0 + k];
         S.acc[base + k] = make_float4(0.f, 0.f, 0.f, 0.f);
         S.gslot[base + k] = g0 + k;
-        S.seg[base + k] = (uint8_t)task;
+        S.sh4[base + k] = sh;
         if (!kSig && kFlux) S.sq[base + k] = 0.f;
     }
 }
@@ -238,7 +243,7 @@ __device__ __forceinline__ void flush(const PairKernelArgs &a, Staged &S, int b0
 }
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
-__global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
+__global__ void __launch_bounds__(kWarps * 32, 5) k_pair_tile(TileArgs T) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Staged *L = reinterpret_cast<Staged *>(smem_raw);
     float *sblob = reinterpret_cast<float *>(smem_raw + sizeof(Staged) * kWarps);
@@ -312,36 +317,35 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
             const int tbeg = with_self ? 0 : nh;
             const int ntgt = end - tbeg;
             with_self = false;
-            const int total = nh * ntgt;
             int qhead = 0, qtail = 0;
-            if (total > 0) {
-                const float inv_nt = 1.0f / (float)ntgt;
-                for (int p0 = 0; p0 < total; p0 += 32) {
-                    const int p = p0 + lane;
-                    bool hit = false;
-                    int i = 0, k = 0;
-                    if (p < total) {
-                        i = (int)(((float)p + 0.5f) * inv_nt);
-                        k = tbeg + (p - i * ntgt);
-                        if (k >= nh || i < k) {
-                            const int sg = S.seg[k];
-                            const float4 pi = S.pos[i], pk = S.pos[k];
+            if (ntgt > 0) {
+                // home particle i (warp-uniform, broadcast) against 32 targets per pass;
+                // self targets (k < nh) only above i
+                for (int i = 0; i < nh; i++) {
+                    const float4 pi4 = S.pos[i];
+                    const float3 xi = make_float3(pi4.x, pi4.y, pi4.z);
+                    const int kfirst = tbeg == 0 ? i + 1 : tbeg;
+                    for (int k0 = kfirst; k0 < end; k0 += 32) {
+                        const int k = k0 + lane;
+                        bool hit = false;
+                        if (k < end) {
+                            const float4 pk = S.pos[k];
+                            const float4 s4 = S.sh4[k];
                             float3 dx;
-                            const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z),
-                                                     make_float3(S.sh[sg][0], S.sh[sg][1], S.sh[sg][2]),
-                                                     make_float3(pk.x, pk.y, pk.z), dx);
+                            const float r2 = pair_r2(xi, make_float3(s4.x, s4.y, s4.z), make_float3(pk.x, pk.y, pk.z), dx);
                             hit = r2 <= P.cutoff2;
                         }
-                    }
-                    const uint32_t m = __ballot_sync(0xffffffffu, hit);
-                    if (hit) S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)k << 16);
-                    qtail += __popc(m);
-                    __syncwarp();
-                    if (qtail - qhead >= 32) {
-                        const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
-                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, spots, blob, true, e, lane, epot, vir);
-                        qhead += 32;
+                        const uint32_t m = __ballot_sync(0xffffffffu, hit);
+                        if (hit)
+                            S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)k << 16);
+                        qtail += __popc(m);
                         __syncwarp();
+                        if (qtail - qhead >= 32) {
+                            const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
+                            eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, spots, blob, true, e, lane, epot, vir);
+                            qhead += 32;
+                            __syncwarp();
+                        }
                     }
                 }
                 if (qtail > qhead) {
