@@ -24,8 +24,8 @@ namespace tfg {
 
 namespace {
 
-constexpr int kWarps = 4;
-constexpr int kCapT = 192;          // staged particles per warp: home cell + neighbour segments
+constexpr int kWarps = 8;
+constexpr int kCapT = 160;          // staged particles per warp: home cell + neighbour segments
 constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
 constexpr int kQ = 64;              // candidate ring queue entries per warp (power of two)
 constexpr int kMaxSmemTable = 4096; // floats of potential table staged per CTA
@@ -37,8 +37,9 @@ struct Staged {
     float4 sh4[kCapT];      // shift of the staged particle's cell as seen from the home cell
     float sh[27][3];        // shift of each task's partner cell (space_getsid)
     uint32_t q[kQ];         // packed hit (i | k << 16), staged indices
-    float sq[kCapT];        // flux increment accumulators (species 0)
 };
+// Flux increment accumulators (species 0) of one warp's staged particles; allocated only
+// by the flux variants, after the Staged array.
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
@@ -56,8 +57,9 @@ struct TileArgs {
 // Evaluate one interacting pair, reference orientation I = part_i (home), K = part_j.
 // Returns the I-side and K-side increments (force xyz, density) in fI / fK.
 template <bool kDPD, bool kFlux, bool kDensity>
-__device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, const PotDev *pots, const float *blob, int I,
-                                          int K, float &epot, float &vir, float4 &fI, float4 &fK) {
+__device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, float *SQ, const PotDev *pots,
+                                          const float *blob, int I, int K, float &epot, float &vir, float4 &fI,
+                                          float4 &fK) {
     const PairKernelArgs &a = T.a;
     const SimParams &P = a.P;
     const float4 pi = S.pos[I], pk = S.pos[K];
@@ -95,8 +97,8 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, const Po
                 const float qq = __fmul_rn(__fmul_rn(F.coef, __fsub_rn(F.target, ssj)), ssi);
                 q = __fmul_rn(q, qq > 0.f ? qq : 0.f);
             }
-            atomicAdd(&S.sq[sa], -q - F.half_decay * ssi);
-            atomicAdd(&S.sq[sb], q - F.half_decay * ssj);
+            atomicAdd(&SQ[sa], -q - F.half_decay * ssi);
+            atomicAdd(&SQ[sb], q - F.half_decay * ssj);
         }
     }
     const PotDev &pot = pots[pidx];
@@ -146,8 +148,9 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, const Po
 // summed into the group's lowest lane.  Every accumulator write is then unique within
 // the batch, so plain shared-memory read-modify-writes suffice.
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
-__device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, const PotDev *pots, const float *blob,
-                                           bool active, uint32_t e, int lane, float &epot, float &vir) {
+__device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, float *SQ, const PotDev *pots,
+                                           const float *blob, bool active, uint32_t e, int lane, float &epot,
+                                           float &vir) {
     const int I = e & 0xffff, K = e >> 16;
     if (kSig) {
         if (active) {
@@ -161,7 +164,7 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, const P
         return;
     }
     float4 fI = make_float4(0.f, 0.f, 0.f, 0.f), fK = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (active) eval_pair<kDPD, kFlux, kDensity>(T, S, pots, blob, I, K, epot, vir, fI, fK);
+    if (active) eval_pair<kDPD, kFlux, kDensity>(T, S, SQ, pots, blob, I, K, epot, vir, fI, fK);
     // I side: segmented inclusive scan over contiguous runs
     const int key = active ? I : 4096 + lane;
 #pragma unroll
@@ -208,20 +211,21 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, const P
 }
 
 template <bool kFlux, bool kSig>
-__device__ __forceinline__ void stage(const PairKernelArgs &a, Staged &S, int base, int g0, int n, int task,
-                                      int lane) {
+__device__ __forceinline__ void stage(const PairKernelArgs &a, Staged &S, float *SQ, int base, int g0, int n,
+                                      int task, int lane) {
     const float4 sh = make_float4(S.sh[task][0], S.sh[task][1], S.sh[task][2], 0.f);
     for (int k = lane; k < n; k += 32) {
         S.pos[base + k] = a.pos[g0 + k];
         S.acc[base + k] = make_float4(0.f, 0.f, 0.f, 0.f);
         S.gslot[base + k] = g0 + k;
         S.sh4[base + k] = sh;
-        if (!kSig && kFlux) S.sq[base + k] = 0.f;
+        if (!kSig && kFlux) SQ[base + k] = 0.f;
     }
 }
 
 template <bool kFlux, bool kSig>
-__device__ __forceinline__ void flush(const PairKernelArgs &a, Staged &S, int b0, int b1, int lane) {
+__device__ __forceinline__ void flush(const PairKernelArgs &a, Staged &S, const float *SQ, int b0, int b1,
+                                      int lane) {
     for (int k = b0 + lane; k < b1; k += 32) {
         const float4 v = S.acc[k];
         const int g = S.gslot[k];
@@ -236,17 +240,18 @@ __device__ __forceinline__ void flush(const PairKernelArgs &a, Staged &S, int b0
         }
         if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(&a.force[g], v);
         if (kFlux) {
-            const float q = S.sq[k];
+            const float q = SQ[k];
             if (q != 0.f) atomicAdd(&a.sq[g], q);
         }
     }
 }
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
-__global__ void __launch_bounds__(kWarps * 32, 5) k_pair_tile(TileArgs T) {
+__global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Staged *L = reinterpret_cast<Staged *>(smem_raw);
-    float *sblob = reinterpret_cast<float *>(smem_raw + sizeof(Staged) * kWarps);
+    float *SQall = reinterpret_cast<float *>(smem_raw + sizeof(Staged) * kWarps);
+    float *sblob = SQall + (kFlux ? kWarps * kCapT : 0);
     const PairKernelArgs &a = T.a;
     const SimParams &P = a.P;
 
@@ -260,6 +265,7 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_pair_tile(TileArgs T) {
 
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     Staged &S = L[wid];
+    float *SQ = SQall + (kFlux ? wid * kCapT : 0);
     float epot = 0.f, vir = 0.f;
     const int nwarps_total = gridDim.x * kWarps;
     const int per = 14 / T.split;
@@ -297,7 +303,7 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_pair_tile(TileArgs T) {
             }
             continue;
         }
-        stage<kFlux, kSig>(a, S, 0, h0, nh, 13, lane);
+        stage<kFlux, kSig>(a, S, SQ, 0, h0, nh, 13, lane);
         __syncwarp();
 
         int t = t0 < 14 ? 14 : t0;     // next neighbour task to stage
@@ -309,7 +315,7 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_pair_tile(TileArgs T) {
                 const int g0 = __shfl_sync(0xffffffffu, my_g0, t - 14);
                 const int nn = __shfl_sync(0xffffffffu, my_n, t - 14);
                 if (end + nn > kCapT) break;
-                if (nn > 0) stage<kFlux, kSig>(a, S, end, g0, nn, t, lane);
+                if (nn > 0) stage<kFlux, kSig>(a, S, SQ, end, g0, nn, t, lane);
                 end += nn;
                 t++;
             }
@@ -342,7 +348,7 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_pair_tile(TileArgs T) {
                         __syncwarp();
                         if (qtail - qhead >= 32) {
                             const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
-                            eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, spots, blob, true, e, lane, epot, vir);
+                            eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, SQ, spots, blob, true, e, lane, epot, vir);
                             qhead += 32;
                             __syncwarp();
                         }
@@ -351,14 +357,14 @@ __global__ void __launch_bounds__(kWarps * 32, 5) k_pair_tile(TileArgs T) {
                 if (qtail > qhead) {
                     const bool act = lane < qtail - qhead;
                     const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
-                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, spots, blob, act, e, lane, epot, vir);
+                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, SQ, spots, blob, act, e, lane, epot, vir);
                 }
                 __syncwarp();
             }
-            flush<kFlux, kSig>(a, S, nh, end, lane);
+            flush<kFlux, kSig>(a, S, SQ, nh, end, lane);
             __syncwarp();
         }
-        flush<kFlux, kSig>(a, S, 0, nh, lane);
+        flush<kFlux, kSig>(a, S, SQ, 0, nh, lane);
         __syncwarp();
     }
     if (kSig) return;
@@ -500,7 +506,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
 void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
-    const size_t base = sizeof(Staged) * kWarps;
+    const size_t base = sizeof(Staged) * kWarps + (kFlux ? sizeof(float) * kWarps * kCapT : 0);
     const size_t smem_max = base + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxTypes * kMaxTypes;
     const int nb = T.a.blob_floats <= kMaxSmemTable ? T.a.blob_floats : 0;
     const size_t smem = base + sizeof(float) * ((nb + 3) & ~3) + sizeof(PotDev) * T.a.P.max_type * T.a.P.max_type;
