@@ -260,6 +260,30 @@ TFG_API int tfg_get_phase_ms(tfg_engine *eng, float ms[4]);
  * helper for roofline reporting; the reference has no counterpart. */
 TFG_API int tfg_probe_fp32_tflops(int device, double *tflops);
 
+/* ---- binning without allocation ----
+ * For callers that cannot allocate device memory (code running inside someone else's
+ * stream capture, plugins confined to a host application's memory pool, real-time loops
+ * where a cudaMalloc/cudaFree would stall the device).  Bins n particles given by GLOBAL
+ * positions exactly as tfg_load_particles does (space_setpartp, tfSpace.cpp:432-475) and
+ * returns, in caller-owned device buffers: the cell index and cell-relative position of
+ * each particle, `order` (particle indices in cell order, by index inside a cell) and
+ * `cell_start` (ncells+1 offsets into `order`).  It calls no cudaMalloc, cudaFree or
+ * allocating library routine: its temporaries live in one file-scope device array of
+ * TFG_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until exit.
+ *   - Limits: n <= TFG_NOALLOC_MAX_PARTICLES and cells[0]*cells[1]*cells[2] <=
+ *     TFG_NOALLOC_MAX_CELLS; larger requests return TFG_E_OVERFLOW and do nothing.
+ *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress
+ *     with that device current); make that first call before any stream capture.
+ *   - All calls share the one array: calls whose work overlaps on the GPU (other streams,
+ *     other host threads) race.  Serialise them, e.g. on one stream.
+ *   - Work is queued on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * No counterpart in the reference (its binning always runs on the host). */
+#define TFG_NOALLOC_MAX_PARTICLES 1048576
+#define TFG_NOALLOC_MAX_CELLS     262144
+#define TFG_NOALLOC_SCRATCH_BYTES ((TFG_NOALLOC_MAX_CELLS + 2 * TFG_NOALLOC_MAX_PARTICLES + 256) * 4)
+TFG_API int tfg_bin_noalloc(const tfg_engine_desc *desc, int n, const float *x_dev, int32_t *cell_dev,
+                            float *xrel_dev, int32_t *order_dev, int32_t *cell_start_dev, void *stream);
+
 /* Library build information: returns a static string. */
 TFG_API const char *tfg_build_info(void);
 

@@ -17,7 +17,8 @@ LIB = os.path.join(BUILD, "libtfg.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["csrc/tfg_engine.cu", "csrc/tfg_pair.cu", "csrc/tfg_pair_tile.cu", "csrc/tfg_probe.cu"]
+CU_SOURCES = ["csrc/tfg_engine.cu", "csrc/tfg_pair.cu", "csrc/tfg_pair_tile.cu", "csrc/tfg_probe.cu",
+              "csrc/tfg_noalloc.cu"]
 CXX_SOURCES = ["host/tfg_potential.cpp"]
 HEADERS = ["csrc/tfg_device.cuh", "csrc/tfg_internal.h"]
 

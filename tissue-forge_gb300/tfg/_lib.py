@@ -56,5 +56,7 @@ def lib():
     L.tfg_get_reductions.argtypes = [E, C.POINTER(abi.Reductions)]
     L.tfg_get_phase_ms.argtypes = [E, C.POINTER(C.c_float)]
     L.tfg_probe_fp32_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.tfg_bin_noalloc.argtypes = [C.POINTER(abi.EngineDesc), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_void_p]
     _lib = L
     return L
