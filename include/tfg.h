@@ -255,6 +255,43 @@ TFG_API int tfg_get_reductions(tfg_engine *eng, tfg_reductions *out);
  * (CUDA events on the engine stream): [0] bin, [1] pair, [2] bonded, [3] advance. */
 TFG_API int tfg_get_phase_ms(tfg_engine *eng, float ms[4]);
 
+/* ---- batches: many independent simulations in one device arena ----
+ * The reference runs one engine per process (the global `_Engine`, tfEngine.cpp); it has no
+ * counterpart to a batch.  An engine made by tfg_engine_create is a batch holding one
+ * simulation, id 0, and the calls above act on it.  tfg_batch_create makes an empty batch;
+ * every simulation added must share its max_type and nr_species, and each has its own space,
+ * cutoff, dt, seed, flags, potentials, fluxes, types, particles, bonds and angles.  All
+ * live simulations step together (tfg_step / tfg_batch_step), one launch per phase for the
+ * whole arena; particle ids, random streams and results of a simulation do not depend on
+ * what else is in the batch.  Additions, removals and loads take effect at the next step or
+ * download, which re-lays the arena out.  Simulation ids are never reused. */
+TFG_API int tfg_batch_create(int device, int max_type, int nr_species, tfg_engine **out);
+TFG_API int tfg_batch_add_sim(tfg_engine *eng, const tfg_engine_desc *desc, int *sim);
+TFG_API int tfg_batch_remove_sim(tfg_engine *eng, int sim);
+TFG_API int tfg_batch_sim_count(const tfg_engine *eng, int *live);
+TFG_API int tfg_batch_step(tfg_engine *eng, int nsteps);
+TFG_API int tfg_batch_set_type(tfg_engine *eng, int sim, int type, int dynamics, float mass);
+TFG_API int tfg_batch_set_potential(tfg_engine *eng, int sim, int ti, int tj, const tfg_potential *p);
+TFG_API int tfg_batch_add_flux(tfg_engine *eng, int sim, int ti, int tj, const tfg_flux *flux);
+TFG_API int tfg_batch_set_species_flags(tfg_engine *eng, int sim, int nr, const uint32_t *flags);
+TFG_API int tfg_batch_set_random_force(tfg_engine *eng, int sim, int type, float mean, float std,
+                                       int duration_steps);
+TFG_API int tfg_batch_load_particles(tfg_engine *eng, int sim, int n, const float *x, const float *v,
+                                     const int32_t *type, const float *radius, const float *imass,
+                                     const uint32_t *flags, const float *species, const float *force_i);
+TFG_API int tfg_batch_load_particles_binned(tfg_engine *eng, int sim, int n, const int32_t *cell,
+                                            const float *xrel, const float *v, const int32_t *type,
+                                            const float *radius, const float *imass, const uint32_t *flags,
+                                            const float *species, const float *force_i);
+TFG_API int tfg_batch_load_bonds(tfg_engine *eng, int sim, int n, const int32_t *i, const int32_t *j,
+                                 const int32_t *slot);
+TFG_API int tfg_batch_load_angles(tfg_engine *eng, int sim, int n, const int32_t *i, const int32_t *j,
+                                  const int32_t *k, const int32_t *slot);
+TFG_API int tfg_batch_get_count(const tfg_engine *eng, int sim, int *n);
+TFG_API int tfg_batch_download(tfg_engine *eng, int sim, float *x, float *xrel, int32_t *cell, float *v,
+                               float *f, float *density, float *species, float *q);
+TFG_API int tfg_batch_get_reductions(tfg_engine *eng, int sim, tfg_reductions *out);
+
 /* Measured FP32 FMA throughput of `device` in TFLOP/s (2 flops per FMA), from a
  * register-only kernel with eight independent FMA chains per thread.  Measurement
  * helper for roofline reporting; the reference has no counterpart. */

@@ -55,11 +55,17 @@ struct FluxSet {
     FluxDev f[kMaxFluxPerPair];
 };
 
-// Per-step kernel parameters of one simulation.
+// Per-step kernel parameters of one simulation.  An engine holds one or more
+// simulations in one device arena: their cells and particles are concatenated, so a
+// simulation owns global cells [cell_off, cell_off + ncells) and global particle ids
+// [id_off, id_off + n).  Per-simulation tables sit at pot_base (potentials and fluxes,
+// max_type^2 entries) and type_base (per-type arrays); its FP64 totals at red_base.
 struct SimParams {
     float h[3], dim[3];
     int32_t cdim[3];
     int32_t ncells;
+    int32_t cell_off, id_off, angle_off;
+    int32_t pot_base, type_base, red_base, spec_base;
     float cutoff, cutoff2;
     float dt, dt_flux;
     float maxx[3], maxx2[3], maxv[3], maxv2[3], h2[3];
@@ -101,11 +107,14 @@ __device__ __forceinline__ float gauss_pair(uint64_t seed, int64_t step, int ida
 }
 
 // ---------------- geometry ----------------
+// Global cell index of the simulation's cell at grid location (i, j, k).
 __device__ __forceinline__ int cell_index(const SimParams &P, int i, int j, int k) {
-    return (i * P.cdim[1] + j) * P.cdim[2] + k;
+    return P.cell_off + (i * P.cdim[1] + j) * P.cdim[2] + k;
 }
 
+// Grid location of global cell c.
 __device__ __forceinline__ void cell_loc(const SimParams &P, int c, int &i, int &j, int &k) {
+    c -= P.cell_off;
     k = c % P.cdim[2];
     int t = c / P.cdim[2];
     j = t % P.cdim[1];

@@ -1,0 +1,132 @@
+// Host-side engine: one device arena holding one or more simulations.
+//
+// A simulation is the reference's engine (source/mdcore/include/tfEngine.h:164-418):
+// space, potentials, fluxes, types, particles, bonds and angles.  The arena concatenates
+// the cells and particles of every live simulation in simulation order, so simulation k
+// owns global cells [cell_off, cell_off+ncells) and, once binned, the particle slots
+// [id_off, id_off+n) (particles are sorted by global cell).  Loads, additions and
+// removals only mark the layout dirty; the next step (or download) re-lays the arena out.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "tfg_kernels.h"
+
+struct SimHost {
+    bool live = true;
+    tfg_engine_desc desc{};
+    tfg::SimParams P{};              // host copy; offsets and pointers filled at layout
+    int maxc = 0;
+    std::vector<float> orig;         // cell origins, 3 * maxc (axis-major)
+    int n = 0;                       // particles of this simulation
+    bool loaded = false;             // a particle load happened
+    bool in_arena = false;           // its particles live in the current arena
+    int arena_slot0 = 0, arena_cell_off = 0;
+    // particle data waiting for the next layout
+    bool pending = false, pending_binned = false;
+    std::vector<float> x, xrel, v, radius, imass, species, force_i;
+    std::vector<int32_t> cell, type;
+    std::vector<uint32_t> flags;
+    // interaction model (max_type^2 potentials and fluxes, per-type arrays)
+    std::vector<tfg::PotDev> pots;
+    std::vector<std::vector<float>> tables;
+    std::vector<tfg::FluxSet> fluxes;
+    std::vector<float4> rforce;
+    std::vector<float> mass;
+    std::vector<int32_t> dyn;
+    std::vector<uint32_t> species_flags;
+    std::vector<int2> bonds;         // local ids
+    std::vector<int32_t> bond_slot;
+    std::vector<int4> angles;        // local ids, w = slot
+    int64_t time = 0;
+};
+
+struct tfg_engine {
+    int device = 0, max_type = 1, nspec = 0, sms = 1;
+    std::vector<SimHost> sims;       // by simulation id; removed ones have live == false
+    std::vector<int> order;          // live simulation ids in arena order (current layout)
+    int n = 0, cap = 0, ncells = 0, cells_cap = 0, cur = 0;
+    tfg::ParticleArrays A[2];
+    float4 *force = nullptr;
+    int32_t *count = nullptr, *start = nullptr, *lidx = nullptr, *tmp_id = nullptr, *tmp_src = nullptr,
+            *dest = nullptr, *slot_of_id = nullptr, *scan_sums = nullptr, *cell_sim = nullptr;
+    int *overflow_list = nullptr, *overflow_count = nullptr;
+    tfg::SimParams *sims_dev = nullptr;
+    int sims_cap = 0;
+    float *corig = nullptr;
+    size_t corig_cap = 0;
+    tfg::PotDev *pots = nullptr;
+    size_t pots_cap = 0;
+    float *blob = nullptr;
+    size_t blob_cap = 0;
+    int blob_floats = 0;
+    tfg::FluxSet *fluxes = nullptr;
+    size_t fluxes_cap = 0;
+    float4 *rforce = nullptr;
+    float *type_mass = nullptr;
+    int32_t *type_dyn = nullptr;
+    size_t types_cap = 0;
+    uint32_t *species_flags = nullptr;
+    size_t spec_cap = 0;
+    int2 *bonds = nullptr;
+    int32_t *bond_slot = nullptr;
+    int4 *angles = nullptr;
+    int nb = 0, na = 0, bcap = 0, acap = 0;
+    tfg::PotDev *bpots = nullptr;
+    float *bblob = nullptr;
+    size_t bblob_cap = 0;
+    std::vector<tfg::PotDev> h_bpots;
+    std::vector<std::vector<float>> h_btables;
+    double *red = nullptr;
+    size_t red_cap = 0;
+    uint32_t *err = nullptr;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaEvent_t ev[5] = {};
+    std::string last_error;
+    bool layout_dirty = true, tables_dirty = true;
+    bool has_dpd = false, has_flux = false;
+    uint32_t flags_all = 0;          // TFG_ENGINE_NO_DENSITY only when every simulation sets it
+    int split = 0;                   // tiled pair pass: warps per home cell (0 = not tuned)
+    int capacity_hint = 0;
+};
+
+namespace tfg {
+
+int fail(tfg_engine *e, int code, const std::string &msg);
+
+// (Re)allocate a device buffer of `count` elements (freeing the old one).
+template <typename T> int dalloc(tfg_engine *eng, T **p, size_t count) {
+    if (*p) { cudaFree(*p); *p = nullptr; }
+    if (count == 0) return TFG_OK;
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * count);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return fail(eng, TFG_E_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    return TFG_OK;
+}
+int check_launch(tfg_engine *eng);
+int read_err(tfg_engine *eng);
+int sim_check(tfg_engine *eng, int sim);        // TFG_OK when `sim` names a live simulation
+int add_sim(tfg_engine *eng, const tfg_engine_desc *d, int *out);
+int commit(tfg_engine *eng);                    // re-lay the arena out and upload tables when dirty
+int bin(tfg_engine *eng, int shuffle);
+int force_pass(tfg_engine *eng, bool bonded, bool timed);
+int one_step(tfg_engine *eng, bool advance, bool timed);
+int autotune(tfg_engine *eng);
+PairKernelArgs pair_args(tfg_engine *eng);
+bool use_tile(const tfg_engine *eng);
+PotDev to_dev(const tfg_potential *p);
+int load_sim(tfg_engine *eng, int sim, int n, const float *xg, const int32_t *cellv, const float *xrel,
+             const float *v, const int32_t *type, const float *radius, const float *imass, const uint32_t *flags,
+             const float *species, const float *force_i);
+int download_sim(tfg_engine *eng, int sim, float *x, float *xrel, int32_t *cell, float *v, float *f, float *dens,
+                 float *species, float *q);
+int reductions_sim(tfg_engine *eng, int sim, tfg_reductions *out);
+void destroy(tfg_engine *eng);
+
+}  // namespace tfg

@@ -38,7 +38,13 @@ enum RedSlot : int {
 };
 
 struct PairKernelArgs {
-    SimParams P;
+    const SimParams *sims;      // per-simulation parameters (device)
+    const int32_t *cell_sim;    // simulation of each global cell (device)
+    int nsims;
+    int ncells;                 // global cells over all simulations
+    int max_type;               // types per simulation (tables are max_type^2 per simulation)
+    int nspec;                  // species per particle (all simulations)
+    uint32_t flags;             // union of the simulations' TFG_ENGINE_* flags
     int n;
     const float4 *pos;
     const float4 *vel;
@@ -51,13 +57,13 @@ struct PairKernelArgs {
     float *sq;
     int cap;
     float4 *force;              // out: f.xyz, number density
-    const PotDev *pots;         // max_type^2
+    const PotDev *pots;         // nsims * max_type^2
     const float *blob;
     int blob_floats;
-    const FluxSet *fluxes;      // max_type^2
-    const float4 *rforce;       // per type: mean, std, duration, enabled
+    const FluxSet *fluxes;      // nsims * max_type^2
+    const float4 *rforce;       // nsims * max_type: mean, std, duration, enabled
     float4 *pforce_out;         // persistent force updated in place (same as pforce)
-    double *red;
+    double *red;                // RED_COUNT per simulation
     uint32_t *err;
     int32_t *sig_count;         // signature mode: interacting neighbours per particle
     uint32_t *sig_hash;         // signature mode: order-independent hash of neighbour ids

@@ -73,8 +73,8 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
     const float *blob = nb ? sblob : a.blob;
 
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const SimParams &P = a.P;
     double red_epot = 0.0, red_vir = 0.0;
+    int red_base = -1;
     if (i < a.n) {
 
     const float4 pi4 = a.pos[i];
@@ -85,6 +85,8 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
     const float ri = axi.x;
     const int idi = __float_as_int(axi.w);
     const int ci = a.cell[i];
+    const SimParams &P = a.sims[a.cell_sim[ci]];
+    red_base = P.red_base;
     int li, lj, lk;
     cell_loc(P, ci, li, lj, lk);
 
@@ -152,7 +154,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
             const float r = __fsqrt_rn(r2);
             if (kDensity) acc.dens += density_w(r, inv_cut, P.self_density);
             const int tj = __float_as_int(pj4.w);
-            const int pidx = ti * P.max_type + tj;
+            const int pidx = P.pot_base + ti * a.max_type + tj;
             if (kHasFlux) {
                 const FluxSet &fs = a.fluxes[pidx];
                 if (fs.count) pair_flux<kHasFlux>(a, fs, i_is_pi, ti, tj, i, j, r, acc);
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
                     const float fd = -pot.dpd_gamma * omega_d * edv;
                     float xi_r = 1.0f;
                     if (!(P.flags & TFG_ENGINE_DPD_REFERENCE_RANDOM))
-                        xi_r = gauss_pair(P.seed, P.time, idi, __float_as_int(axj.w));
+                        xi_r = gauss_pair(P.seed, P.time, idi - P.id_off, __float_as_int(axj.w) - P.id_off);
                     const float fr = pot.dpd_sigma * omega_c * xi_r * P.dpd_delta;
                     const float ftot = fc + fd + fr;
                     // part_i.f += F e ; part_j.f -= F e
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
     } else {
         a.force[i] = make_float4(acc.fx, acc.fy, acc.fz, acc.dens);
         if (kHasFlux) {
-            for (int s = 0; s < P.nspec; s++) a.sq[s * a.cap + i] += acc.q[s];
+            for (int s = 0; s < a.nspec; s++) a.sq[s * a.cap + i] += acc.q[s];
         }
         red_epot = (double)acc.epot;
         red_vir = (double)acc.vir;
@@ -218,14 +220,21 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
     }  // i < n
     if (kSig) return;
 
-    // FP64 warp reduction of energy and virial, one atomic per warp.
-    for (int o = 16; o > 0; o >>= 1) {
-        red_epot += __shfl_down_sync(0xffffffffu, red_epot, o);
-        red_vir += __shfl_down_sync(0xffffffffu, red_vir, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-        if (red_epot != 0.0) atomicAdd(&a.red[RED_EPOT_NONBOND], red_epot);
-        if (red_vir != 0.0) atomicAdd(&a.red[RED_VIRIAL], red_vir);
+    // FP64 warp reduction of energy and virial into each simulation's totals: one atomic
+    // per warp when the warp's particles belong to one simulation, else one per lane.
+    const int rb0 = __shfl_sync(0xffffffffu, red_base, 0);
+    if (__all_sync(0xffffffffu, red_base == rb0 || red_base < 0)) {
+        for (int o = 16; o > 0; o >>= 1) {
+            red_epot += __shfl_down_sync(0xffffffffu, red_epot, o);
+            red_vir += __shfl_down_sync(0xffffffffu, red_vir, o);
+        }
+        if ((threadIdx.x & 31) == 0 && rb0 >= 0) {
+            if (red_epot != 0.0) atomicAdd(&a.red[rb0 + RED_EPOT_NONBOND], red_epot);
+            if (red_vir != 0.0) atomicAdd(&a.red[rb0 + RED_VIRIAL], red_vir);
+        }
+    } else if (red_base >= 0) {
+        if (red_epot != 0.0) atomicAdd(&a.red[red_base + RED_EPOT_NONBOND], red_epot);
+        if (red_vir != 0.0) atomicAdd(&a.red[red_base + RED_VIRIAL], red_vir);
     }
 }
 
@@ -242,9 +251,8 @@ void launch_pair(const PairKernelArgs &a, cudaStream_t s) {
     if (a.n <= 0) return;
     const int blocks = (a.n + kPairThreads - 1) / kPairThreads;
     const size_t smem = (a.blob_floats <= kMaxSmemBlob ? a.blob_floats : 0) * sizeof(float);
-    bool flux = false;
-    for (int k = 0; k < a.P.max_type * a.P.max_type && !flux; k++) flux = a.P.nspec > 0;
-    const bool dens = !(a.P.flags & TFG_ENGINE_NO_DENSITY);
+    const bool flux = a.nspec > 0 && a.has_flux;
+    const bool dens = !(a.flags & TFG_ENGINE_NO_DENSITY);
     if (flux) {
         if (dens) k_pair_stencil<true, true><<<blocks, kPairThreads, smem, s>>>(a);
         else k_pair_stencil<true, false><<<blocks, kPairThreads, smem, s>>>(a);

@@ -29,6 +29,7 @@ constexpr int kCapT = 160;          // staged particles per warp: home cell + ne
 constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
 constexpr int kQ = 64;              // candidate ring queue entries per warp (power of two)
 constexpr int kMaxSmemTable = 4096; // floats of potential table staged per CTA
+constexpr int kMaxSmemPots = 64;    // potential descriptors staged per CTA (all simulations)
 
 struct Staged {
     float4 pos[kCapT];      // cell-relative position; w = type bits
@@ -57,11 +58,10 @@ struct TileArgs {
 // Evaluate one interacting pair, reference orientation I = part_i (home), K = part_j.
 // Returns the I-side and K-side increments (force xyz, density) in fI / fK.
 template <bool kDPD, bool kFlux, bool kDensity>
-__device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, float *SQ, const PotDev *pots,
-                                          const float *blob, int I, int K, float &epot, float &vir, float4 &fI,
-                                          float4 &fK) {
+__device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P, Staged &S, float *SQ,
+                                          const PotDev *pots, const float *blob, int I, int K, float &epot,
+                                          float &vir, float4 &fI, float4 &fK) {
     const PairKernelArgs &a = T.a;
-    const SimParams &P = a.P;
     const float4 pi = S.pos[I], pk = S.pos[K];
     const float4 s4 = S.sh4[K];
     const float3 sh = make_float3(s4.x, s4.y, s4.z);
@@ -74,7 +74,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, float *S
         fK.w += w;
     }
     const int ti = __float_as_int(pi.w), tk = __float_as_int(pk.w);
-    const int pidx = ti * P.max_type + tk;
+    const int pidx = P.pot_base + ti * a.max_type + tk;
     const int gi = S.gslot[I], gk = S.gslot[K];
     if (kFlux) {
         const FluxSet &fs = a.fluxes[pidx];
@@ -130,7 +130,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, float *S
             const float edv = ex * (vi.x - vk.x) + ey * (vi.y - vk.y) + ez * (vi.z - vk.z);
             float xi_r = 1.0f;
             if (!(P.flags & TFG_ENGINE_DPD_REFERENCE_RANDOM))
-                xi_r = gauss_pair(P.seed, P.time, __float_as_int(axi.w), __float_as_int(axk.w));
+                xi_r = gauss_pair(P.seed, P.time, __float_as_int(axi.w) - P.id_off, __float_as_int(axk.w) - P.id_off);
             const float ftot = pot.dpd_alpha * omega_c - pot.dpd_gamma * omega_c * omega_c * edv +
                                pot.dpd_sigma * omega_c * xi_r * P.dpd_delta;
             const float wx = ftot * ex, wy = ftot * ey, wz = ftot * ez;
@@ -148,9 +148,9 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, Staged &S, float *S
 // summed into the group's lowest lane.  Every accumulator write is then unique within
 // the batch, so plain shared-memory read-modify-writes suffice.
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
-__device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, float *SQ, const PotDev *pots,
-                                           const float *blob, bool active, uint32_t e, int lane, float &epot,
-                                           float &vir) {
+__device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P, Staged &S, float *SQ,
+                                           const PotDev *pots, const float *blob, bool active, uint32_t e, int lane,
+                                           float &epot, float &vir) {
     const int I = e & 0xffff, K = e >> 16;
     if (kSig) {
         if (active) {
@@ -164,7 +164,7 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, float *
         return;
     }
     float4 fI = make_float4(0.f, 0.f, 0.f, 0.f), fK = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (active) eval_pair<kDPD, kFlux, kDensity>(T, S, SQ, pots, blob, I, K, epot, vir, fI, fK);
+    if (active) eval_pair<kDPD, kFlux, kDensity>(T, P, S, SQ, pots, blob, I, K, epot, vir, fI, fK);
     // I side: segmented inclusive scan over contiguous runs
     const int key = active ? I : 4096 + lane;
 #pragma unroll
@@ -210,6 +210,21 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, Staged &S, float *
     }
 }
 
+// Add a warp's FP32 energy and virial partials to a simulation's FP64 totals.
+__device__ __forceinline__ void flush_red(double *red, int rb, float &epot, float &vir, int lane) {
+    double de = epot, dv = vir;
+    for (int o = 16; o > 0; o >>= 1) {
+        de += __shfl_down_sync(0xffffffffu, de, o);
+        dv += __shfl_down_sync(0xffffffffu, dv, o);
+    }
+    if (lane == 0 && rb >= 0) {
+        if (de != 0.0) atomicAdd(&red[rb + RED_EPOT_NONBOND], de);
+        if (dv != 0.0) atomicAdd(&red[rb + RED_VIRIAL], dv);
+    }
+    epot = 0.f;
+    vir = 0.f;
+}
+
 template <bool kFlux, bool kSig>
 __device__ __forceinline__ void stage(const PairKernelArgs &a, Staged &S, float *SQ, int base, int g0, int n,
                                       int task, int lane) {
@@ -253,28 +268,37 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
     float *SQall = reinterpret_cast<float *>(smem_raw + sizeof(Staged) * kWarps);
     float *sblob = SQall + (kFlux ? kWarps * kCapT : 0);
     const PairKernelArgs &a = T.a;
-    const SimParams &P = a.P;
 
     const int nb = a.blob_floats <= kMaxSmemTable ? a.blob_floats : 0;
     for (int k = threadIdx.x; k < nb; k += blockDim.x) sblob[k] = a.blob[k];
-    PotDev *spots = reinterpret_cast<PotDev *>(sblob + ((nb + 3) & ~3));
-    const int npots = P.max_type * P.max_type;
-    for (int k = threadIdx.x; k < npots; k += blockDim.x) spots[k] = a.pots[k];
+    PotDev *spot_smem = reinterpret_cast<PotDev *>(sblob + ((nb + 3) & ~3));
+    const int npots = a.nsims * a.max_type * a.max_type;
+    const bool stage_pots = npots <= kMaxSmemPots;
+    if (stage_pots)
+        for (int k = threadIdx.x; k < npots; k += blockDim.x) spot_smem[k] = a.pots[k];
     __syncthreads();
     const float *blob = nb ? sblob : a.blob;
+    const PotDev *spots = stage_pots ? spot_smem : a.pots;
 
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     Staged &S = L[wid];
     float *SQ = SQall + (kFlux ? wid * kCapT : 0);
     float epot = 0.f, vir = 0.f;
+    int cur_rb = -1;
     const int nwarps_total = gridDim.x * kWarps;
     const int per = 14 / T.split;
-    const int nitems = P.ncells * T.split;
+    const int nitems = a.ncells * T.split;
 
     for (int item = blockIdx.x * kWarps + wid; item < nitems; item += nwarps_total) {
         const int home = item / T.split, grp = item - home * T.split;
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         if (nh == 0) continue;
+        const SimParams &P = a.sims[a.cell_sim[home]];
+        if (!kSig && P.red_base != cur_rb) {
+            flush_red(a.red, cur_rb, epot, vir, lane);
+            cur_rb = P.red_base;
+        }
+        const float cutoff2 = P.cutoff2;
         const int t0 = 13 + grp * per, t1 = t0 + per;
         int li, lj, lk;
         cell_loc(P, home, li, lj, lk);
@@ -339,7 +363,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                             const float4 s4 = S.sh4[k];
                             float3 dx;
                             const float r2 = pair_r2(xi, make_float3(s4.x, s4.y, s4.z), make_float3(pk.x, pk.y, pk.z), dx);
-                            hit = r2 <= P.cutoff2;
+                            hit = r2 <= cutoff2;
                         }
                         const uint32_t m = __ballot_sync(0xffffffffu, hit);
                         if (hit)
@@ -348,7 +372,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                         __syncwarp();
                         if (qtail - qhead >= 32) {
                             const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
-                            eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, SQ, spots, blob, true, e, lane, epot, vir);
+                            eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, SQ, spots, blob, true, e, lane, epot, vir);
                             qhead += 32;
                             __syncwarp();
                         }
@@ -357,7 +381,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                 if (qtail > qhead) {
                     const bool act = lane < qtail - qhead;
                     const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
-                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, S, SQ, spots, blob, act, e, lane, epot, vir);
+                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, SQ, spots, blob, act, e, lane, epot, vir);
                 }
                 __syncwarp();
             }
@@ -368,15 +392,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
         __syncwarp();
     }
     if (kSig) return;
-    double de = epot, dv = vir;
-    for (int o = 16; o > 0; o >>= 1) {
-        de += __shfl_down_sync(0xffffffffu, de, o);
-        dv += __shfl_down_sync(0xffffffffu, dv, o);
-    }
-    if (lane == 0) {
-        if (de != 0.0) atomicAdd(&a.red[RED_EPOT_NONBOND], de);
-        if (dv != 0.0) atomicAdd(&a.red[RED_VIRIAL], dv);
-    }
+    flush_red(a.red, cur_rb, epot, vir, lane);
 }
 
 // Home cells whose own or neighbour population exceeds the staging capacity: one warp
@@ -385,13 +401,13 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
 __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
     const PairKernelArgs &a = T.a;
-    const SimParams &P = a.P;
     const int lane = threadIdx.x & 31;
     const int nlist = *T.overflow_count;
     float epot = 0.f, vir = 0.f;
     for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nlist; w += (gridDim.x * blockDim.x) >> 5) {
         const int home = T.overflow_list[w];
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
+        const SimParams &P = a.sims[a.cell_sim[home]];
         int li, lj, lk;
         cell_loc(P, home, li, lj, lk);
         for (int d = 13; d < 27; d++) {
@@ -433,7 +449,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                     fj.w = wd;
                 }
                 const int ti = __float_as_int(pi.w), tj = __float_as_int(pj.w);
-                const int pidx = ti * P.max_type + tj;
+                const int pidx = P.pot_base + ti * a.max_type + tj;
                 if (kFlux) {
                     const FluxSet &fs = a.fluxes[pidx];
                     for (int k = 0; k < fs.count; k++) {
@@ -479,7 +495,8 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                         const float edv = ex * (vi.x - vj.x) + ey * (vi.y - vj.y) + ez * (vi.z - vj.z);
                         float xi_r = 1.0f;
                         if (!(P.flags & TFG_ENGINE_DPD_REFERENCE_RANDOM))
-                            xi_r = gauss_pair(P.seed, P.time, __float_as_int(axi.w), __float_as_int(axj.w));
+                            xi_r = gauss_pair(P.seed, P.time, __float_as_int(axi.w) - P.id_off,
+                                              __float_as_int(axj.w) - P.id_off);
                         const float ftot = pot.dpd_alpha * omega_c - pot.dpd_gamma * omega_c * omega_c * edv +
                                            pot.dpd_sigma * omega_c * xi_r * P.dpd_delta;
                         fi.x += ftot * ex; fi.y += ftot * ey; fi.z += ftot * ez;
@@ -491,25 +508,17 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                 atomicAdd(&a.force[gj], fj);
             }
         }
-    }
-    if (kSig) return;
-    double de = epot, dv = vir;
-    for (int o = 16; o > 0; o >>= 1) {
-        de += __shfl_down_sync(0xffffffffu, de, o);
-        dv += __shfl_down_sync(0xffffffffu, dv, o);
-    }
-    if (lane == 0) {
-        if (de != 0.0) atomicAdd(&a.red[RED_EPOT_NONBOND], de);
-        if (dv != 0.0) atomicAdd(&a.red[RED_VIRIAL], dv);
+        if (!kSig) flush_red(a.red, P.red_base, epot, vir, lane);
     }
 }
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
 void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
     const size_t base = sizeof(Staged) * kWarps + (kFlux ? sizeof(float) * kWarps * kCapT : 0);
-    const size_t smem_max = base + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxTypes * kMaxTypes;
+    const size_t smem_max = base + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxSmemPots;
     const int nb = T.a.blob_floats <= kMaxSmemTable ? T.a.blob_floats : 0;
-    const size_t smem = base + sizeof(float) * ((nb + 3) & ~3) + sizeof(PotDev) * T.a.P.max_type * T.a.P.max_type;
+    const int npots = T.a.nsims * T.a.max_type * T.a.max_type;
+    const size_t smem = base + sizeof(float) * ((nb + 3) & ~3) + sizeof(PotDev) * (npots <= kMaxSmemPots ? npots : 0);
     static bool configured = false;
     static size_t occ_smem = 0;
     static int per_sm = 1;
@@ -524,7 +533,7 @@ void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
         if (per_sm < 1) per_sm = 1;
         occ_smem = smem;
     }
-    const int want = (T.a.P.ncells * T.split + kWarps - 1) / kWarps;
+    const int want = (T.a.ncells * T.split + kWarps - 1) / kWarps;
     const int grid = std::max(1, std::min(want, sms * per_sm));
     k_pair_tile<kDPD, kFlux, kDensity, kSig><<<grid, kWarps * 32, smem, s>>>(T);
     k_pair_overflow<kDPD, kFlux, kDensity, kSig><<<sms, 256, 0, s>>>(T);
@@ -543,8 +552,8 @@ void launch_pair_tile(const PairKernelArgs &a, int *overflow_list, int *overflow
     T.split = (split == 1 || split == 2 || split == 7 || split == 14) ? split : 1;
     cudaMemsetAsync(overflow_count, 0, sizeof(int), s);
     if (a.n <= 0) return;
-    const bool dpd = a.has_dpd, flux = a.P.nspec > 0 && a.has_flux;
-    const bool dens = !(a.P.flags & TFG_ENGINE_NO_DENSITY);
+    const bool dpd = a.has_dpd, flux = a.nspec > 0 && a.has_flux;
+    const bool dens = !(a.flags & TFG_ENGINE_NO_DENSITY);
     if (signature) {
         launch_variant<false, false, false, true>(T, s, sms);
         return;

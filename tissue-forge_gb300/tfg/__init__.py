@@ -7,4 +7,4 @@ reference's Potential / Fluxes / Bond / engine objects for Python callers.
 from . import abi, configs  # noqa: F401
 from ._lib import lib, lib_path  # noqa: F401
 from .potentials import Potential  # noqa: F401
-from .engine import Engine, TfgError  # noqa: F401
+from .engine import Batch, Engine, Sim, TfgError  # noqa: F401

@@ -58,5 +58,25 @@ def lib():
     L.tfg_probe_fp32_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.tfg_bin_noalloc.argtypes = [C.POINTER(abi.EngineDesc), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.c_void_p]
+    L.tfg_batch_create.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(E)]
+    L.tfg_batch_add_sim.argtypes = [E, C.POINTER(abi.EngineDesc), C.POINTER(C.c_int)]
+    L.tfg_batch_remove_sim.argtypes = [E, C.c_int]
+    L.tfg_batch_sim_count.argtypes = [E, C.POINTER(C.c_int)]
+    L.tfg_batch_step.argtypes = [E, C.c_int]
+    L.tfg_batch_set_type.argtypes = [E, C.c_int, C.c_int, C.c_int, C.c_float]
+    L.tfg_batch_set_potential.argtypes = [E, C.c_int, C.c_int, C.c_int, abi.P_POT]
+    L.tfg_batch_add_flux.argtypes = [E, C.c_int, C.c_int, C.c_int, C.POINTER(abi.Flux)]
+    L.tfg_batch_set_species_flags.argtypes = [E, C.c_int, C.c_int, abi.U_P]
+    L.tfg_batch_set_random_force.argtypes = [E, C.c_int, C.c_int, C.c_float, C.c_float, C.c_int]
+    L.tfg_batch_load_particles.argtypes = [E, C.c_int, C.c_int, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P,
+                                           abi.U_P, abi.F_P, abi.F_P]
+    L.tfg_batch_load_particles_binned.argtypes = [E, C.c_int, C.c_int, abi.I_P, abi.F_P, abi.F_P, abi.I_P,
+                                                  abi.F_P, abi.F_P, abi.U_P, abi.F_P, abi.F_P]
+    L.tfg_batch_load_bonds.argtypes = [E, C.c_int, C.c_int, abi.I_P, abi.I_P, abi.I_P]
+    L.tfg_batch_load_angles.argtypes = [E, C.c_int, C.c_int, abi.I_P, abi.I_P, abi.I_P, abi.I_P]
+    L.tfg_batch_get_count.argtypes = [E, C.c_int, C.POINTER(C.c_int)]
+    L.tfg_batch_download.argtypes = [E, C.c_int, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P,
+                                     abi.F_P]
+    L.tfg_batch_get_reductions.argtypes = [E, C.c_int, C.POINTER(abi.Reductions)]
     _lib = L
     return L

@@ -170,6 +170,141 @@ class Engine:
         return list(ms)
 
 
+class Batch(Engine):
+    """Many independent simulations in one device arena (tfg_batch_*).  Engine-wide calls
+    (step, sync, autotune, set_split, set_stream, phase_ms, set_bonded_potential) act on the
+    whole batch; per-simulation calls go through the Sim handles add_sim returns."""
+
+    def __init__(self, max_type, nr_species=0, device=0):
+        self.L = lib()
+        self.h = C.c_void_p()
+        self.nspec = nr_species
+        self.max_type = max_type
+        rc = self.L.tfg_batch_create(device, max_type, nr_species, C.byref(self.h))
+        if rc != 0:
+            raise TfgError(rc, "tfg_batch_create")
+        self.sims = {}
+        self._keep = []
+
+    def add_sim(self, desc):
+        sid = C.c_int()
+        self._chk(self.L.tfg_batch_add_sim(self.h, C.byref(desc), C.byref(sid)), "batch_add_sim")
+        sim = Sim(self, sid.value, desc)
+        self.sims[sid.value] = sim
+        return sim
+
+    def remove_sim(self, sim):
+        sid = sim.sid if isinstance(sim, Sim) else int(sim)
+        self._chk(self.L.tfg_batch_remove_sim(self.h, sid), "batch_remove_sim")
+        self.sims.pop(sid, None)
+
+    @property
+    def n(self):
+        """Particles of all loaded simulations (the length of pair_signature's arrays)."""
+        return sum(s.n for s in self.sims.values())
+
+    @n.setter
+    def n(self, v):
+        pass
+
+    def live_count(self):
+        v = C.c_int()
+        self._chk(self.L.tfg_batch_sim_count(self.h, C.byref(v)), "batch_sim_count")
+        return v.value
+
+    def step(self, n=1, sync=True):
+        self._chk(self.L.tfg_batch_step(self.h, n), "batch_step")
+        if sync:
+            self.sync()
+
+
+class Sim:
+    """One simulation of a Batch; method names match Engine's per-simulation calls."""
+
+    def __init__(self, batch, sid, desc):
+        self.b = batch
+        self.L = batch.L
+        self.sid = sid
+        self.desc = desc
+        self.nspec = desc.nr_species
+        self.n = 0
+
+    def _chk(self, rc, what):
+        self.b._chk(rc, what)
+
+    def set_type(self, t, dynamics, mass=1.0):
+        self._chk(self.L.tfg_batch_set_type(self.b.h, self.sid, t, dynamics, mass), "batch_set_type")
+
+    def set_potential(self, ti, tj, pot):
+        ptr = pot.ptr if isinstance(pot, Potential) else pot
+        self._chk(self.L.tfg_batch_set_potential(self.b.h, self.sid, ti, tj, ptr), "batch_set_potential")
+
+    def add_flux(self, ti, tj, flux):
+        self._chk(self.L.tfg_batch_add_flux(self.b.h, self.sid, ti, tj, C.byref(flux)), "batch_add_flux")
+
+    def set_species_flags(self, flags):
+        a = np.ascontiguousarray(flags, np.uint32)
+        self._chk(self.L.tfg_batch_set_species_flags(self.b.h, self.sid, len(a), _up(a)), "batch_set_species_flags")
+
+    def set_random_force(self, t, mean, std, duration_steps):
+        self._chk(self.L.tfg_batch_set_random_force(self.b.h, self.sid, t, mean, std, duration_steps),
+                  "batch_set_random_force")
+
+    def set_bonded_potential(self, slot, pot):
+        self.b.set_bonded_potential(slot, pot)
+
+    def load(self, x, v=None, type=None, radius=None, imass=None, flags=None, species=None, force_i=None):
+        x = np.ascontiguousarray(x, np.float32)
+        self.n = x.shape[0]
+        v, radius, imass, species, force_i = (_conv(a, np.float32) for a in (v, radius, imass, species, force_i))
+        type = _conv(type, np.int32)
+        flags = _conv(flags, np.uint32)
+        self._chk(self.L.tfg_batch_load_particles(self.b.h, self.sid, self.n, _fp(x), _fp(v), _ip(type),
+                                                  _fp(radius), _fp(imass), _up(flags), _fp(species),
+                                                  _fp(force_i)), "batch_load_particles")
+
+    def load_binned(self, cell, xrel, v=None, type=None, radius=None, imass=None, flags=None, species=None,
+                    force_i=None):
+        cell = np.ascontiguousarray(cell, np.int32)
+        xrel = np.ascontiguousarray(xrel, np.float32)
+        self.n = cell.shape[0]
+        v, radius, imass, species, force_i = (_conv(a, np.float32) for a in (v, radius, imass, species, force_i))
+        type = _conv(type, np.int32)
+        flags = _conv(flags, np.uint32)
+        self._chk(self.L.tfg_batch_load_particles_binned(self.b.h, self.sid, self.n, _ip(cell), _fp(xrel), _fp(v),
+                                                         _ip(type), _fp(radius), _fp(imass), _up(flags),
+                                                         _fp(species), _fp(force_i)), "batch_load_particles_binned")
+
+    def load_bonds(self, i, j, slot=None):
+        i, j = (np.ascontiguousarray(a, np.int32) for a in (i, j))
+        slot = _conv(slot, np.int32)
+        self._chk(self.L.tfg_batch_load_bonds(self.b.h, self.sid, len(i), _ip(i), _ip(j), _ip(slot)),
+                  "batch_load_bonds")
+
+    def load_angles(self, i, j, k, slot=None):
+        i, j, k = (np.ascontiguousarray(a, np.int32) for a in (i, j, k))
+        slot = _conv(slot, np.int32)
+        self._chk(self.L.tfg_batch_load_angles(self.b.h, self.sid, len(i), _ip(i), _ip(j), _ip(k), _ip(slot)),
+                  "batch_load_angles")
+
+    def download(self):
+        n, ns = self.n, self.nspec
+        out = dict(x=np.zeros((n, 3), np.float32), xrel=np.zeros((n, 3), np.float32),
+                   cell=np.zeros(n, np.int32), v=np.zeros((n, 3), np.float32), f=np.zeros((n, 3), np.float32),
+                   density=np.zeros(n, np.float32), species=np.zeros((n, max(ns, 0)), np.float32),
+                   q=np.zeros((n, max(ns, 0)), np.float32))
+        self._chk(self.L.tfg_batch_download(self.b.h, self.sid, _fp(out["x"]), _fp(out["xrel"]), _ip(out["cell"]),
+                                            _fp(out["v"]), _fp(out["f"]), _fp(out["density"]),
+                                            _fp(out["species"]) if ns else None, _fp(out["q"]) if ns else None),
+                  "batch_download")
+        return out
+
+    def reductions(self):
+        r = abi.Reductions()
+        self._chk(self.L.tfg_batch_get_reductions(self.b.h, self.sid, C.byref(r)), "batch_get_reductions")
+        return r
+
+
 def setup_model(eng, w, keep=None):
     """Apply a configs.Workload's interaction model and particles to an engine-like object
     (the GPU Engine or the CPU oracle share these method names).  Returns the Potential
