@@ -2,25 +2,33 @@
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl tfg|reference]
 
-A "step" is one full engine step (re-bin, fused pair pass, bonded, advance, reductions)
-over one simulation held resident in HBM.  The default workload is the DPD-droplets
-configuration (100,000 particles, box 40, cutoff 1, DPD + Fickian flux).  Between timed
-steps the L2 is flushed by writing a 256 MiB buffer (the working set is smaller than L2).
+Default workload "ensemble": 256 independent cell-sorting simulations (particle counts
+log-uniform in [500, 50,000], A-B Morse depth uniform in [0.1, 2.0], box side for density
+0.5, Gaussian random force 0.1) held in one device arena.  A "step" is one engine step of
+every simulation of the batch (re-bin, fused pair pass, advance, FP64 per-simulation
+totals), K steps replayed from captured CUDA graphs.  The arena (about 2.75M particles,
+several hundred MB) is larger than L2, so L2 is not flushed.
 
-value  = particle-steps/s with state resident on the device (CUDA events on the engine's
-         stream, summed over the K timed steps, max over ranks).
-e2e    = the same metric through the reference-facing C ABI with host buffers: every step
-         uploads the particle state from pinned host memory (tfg_load_particles_binned),
-         runs one step and downloads positions, velocities and species (tfg_download).
-roofline: the pair kernel against the measured FP32 FMA peak (tfg_probe_fp32_tflops).
+value     = batched particle-steps/s (sum of N_i over the batch x K / CUDA-event time on
+            the engine's stream, max over ranks).
+plain_gpu = the same simulations run one at a time, each in its own engine (same kernels,
+            same graphs), the "plain one-simulation-at-a-time GPU path".
+e2e       = the whole job through the C ABI with host buffers: load every simulation from
+            host arrays, run --e2e-steps steps, download positions and velocities.
+serving   = a bounded sample of the served stream (Poisson arrivals at 200/s, 60/40 cell
+            sorting / DPD droplets, 1,000-200,000 particles, 100-5,000 steps): achieved
+            particle-steps/s, p50/p99 completion latency.
+roofline  = the pair kernel against the measured FP32 FMA peak (tfg_probe_fp32_tflops), and
+            the whole step against the measured HBM bandwidth.
 cpu_baseline: the CPU restatement of the reference engine (threaded, all host cores) on a
-         bounded sample of the same workload.
+            bounded sample of the same simulations.
+Other workloads (--workload dpd_droplets | bonded_fluid | cell_sorting) time one
+simulation with L2 flushed between steps; --workload served runs only the served stream.
 --impl reference: the CPU restatement of the reference engine timed on the host cores (the
-         reference itself cannot be built: its Magnum/Corrade/libsbml submodules are empty
-         and it needs GL/GLFW/assimp).
-For N>1 (torchrun) every rank runs an independent replica of the workload (the path has no
-data-path exchange between simulations): scaling "weak", value = all ranks' particle-steps
-divided by the slowest rank's time.
+            reference itself cannot be built: its Magnum/Corrade/libsbml submodules are
+            empty and it needs GL/GLFW/assimp).
+For N>1 (torchrun) every rank runs an independent replica (no data-path exchange between
+simulations): scaling "weak", value = all ranks' particle-steps / the slowest rank's time.
 """
 import argparse
 import json
@@ -37,6 +45,11 @@ sys.path.insert(0, os.path.join(ROOT, "tissue-forge_gb300"))
 import numpy as np  # noqa: E402
 
 WORKLOADS = {
+    "ensemble": dict(desc="batched ensemble: 256 independent cell-sorting simulations, N log-uniform in "
+                          "[500, 50000], A-B Morse depth U[0.1, 2.0], density 0.5, cutoff 3, random force 0.1, "
+                          "overdamped dt 0.005", bytes_per_particle=48),
+    "served": dict(desc="served stream: Poisson arrivals 200/s, 60/40 cell-sorting / DPD-droplet simulations, "
+                        "N log-uniform in [1000, 200000], steps U[100, 5000]", bytes_per_particle=64),
     "dpd_droplets": dict(desc="DPD droplets with Fickian flux: 100,000 particles, box 40, cutoff 1, "
                               "alpha 10 gamma 4.5 sigma 3, Fick k 0.5, dt 0.01", bytes_per_particle=88),
     "bonded_fluid": dict(desc="LJ 12-6 fluid in chains of 16 with harmonic bonds and angles: 2,000,000 particles "
@@ -155,45 +168,418 @@ def cpu_reference_rate(w, threads, budget_s, max_steps=200):
     return w.n * steps / dt, steps, dt
 
 
+
+def hbm_peak():
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def clock_path(name):
+    d = os.path.join(ROOT, "gpurun_out")
+    return os.path.join(d if os.path.isdir(d) else "/tmp", name)
+
+
+def fp32_peak(dev):
+    import ctypes as C
+    from tfg import lib
+    peak = C.c_double(0.0)
+    lib().tfg_probe_fp32_tflops(dev, C.byref(peak))
+    return peak.value
+
+
+def launches_per_step(has_bonds=False, has_angles=False):
+    # tick, 7 binning kernels (count, 3 scan passes, place, rank, scatter), the tiled pair
+    # kernel and its overflow kernel, bonds, angles, advance
+    return 1 + 7 + 2 + int(has_bonds) + int(has_angles) + 1
+
+
+def ensemble_sample(ws, count):
+    """Every k-th simulation of the ensemble, `count` of them (the bounded CPU sample)."""
+    k = max(1, len(ws) // count)
+    return ws[::k][:count]
+
+
+def cpu_rate_sims(ws, threads, budget_s, max_steps=50):
+    """Particle-steps/s of the CPU restatement over simulations run one after another."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from tfg.engine import setup_model
+    tot_ps, tot_t, steps_done = 0.0, 0.0, []
+    per_sim = budget_s / max(1, len(ws))
+    for w in ws:
+        e = O.OracleEngine(w.desc(), 0, threads, signature=False)
+        keep = setup_model(e, w)
+        e.step(1)
+        t0 = time.perf_counter()
+        k = 0
+        while k < max_steps:
+            e.step(1)
+            k += 1
+            if time.perf_counter() - t0 > per_sim:
+                break
+        dt = time.perf_counter() - t0
+        tot_ps += w.n * k
+        tot_t += dt
+        steps_done.append(k)
+        del keep, e
+    return tot_ps / tot_t, steps_done, tot_t
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    w = make_workload(args.workload, 0, args.n or None, args.relax)
     threads = os.cpu_count() or 1
-    budget = 20.0
-    rates = []
-    for k in range(args.warmup + args.steps):
-        rate, steps, dt = cpu_reference_rate(w, threads, budget / max(1, args.steps), max_steps=50)
-        if k >= args.warmup:
-            rates.append((rate, steps, dt))
-    total_ps = sum(r[1] for r in rates) * w.n
-    total_t = sum(r[2] for r in rates)
-    value = total_ps / total_t
+    if args.workload in ("ensemble", "served"):
+        from tfg import configs
+        ws = ensemble_sample(configs.ensemble(count=args.sims, seed=0), 16)
+        sample = ("16 of the 256 simulations (every 16th, %d particles) advanced one engine step each per "
+                  "timed step, threaded oracle" % sum(w.n for w in ws))
+    else:
+        ws = [make_workload(args.workload, 0, args.n or None, args.relax)]
+        sample = "one engine step of the %s workload per timed step, threaded oracle" % args.workload
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from tfg.engine import setup_model
+    engines = []
+    for w in ws:
+        e = O.OracleEngine(w.desc(), 0, threads, signature=False)
+        engines.append((e, setup_model(e, w), w.n))
+    for k in range(args.warmup):
+        for e, _, _ in engines:
+            e.step(1)
+    ps, t = 0.0, 0.0
+    steps = min(args.steps, 30)
+    for k in range(steps):
+        t0 = time.perf_counter()
+        for e, _, n in engines:
+            e.step(1)
+            ps += n
+        t += time.perf_counter() - t0
+    value = ps / t
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / max(1, sum(r[1] for r in rates)),
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"], "n_particles": w.n},
+        "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"],
+                   "n_particles_sampled": sum(w.n for w in ws)},
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                         "sample": "%d engine steps of the %s workload per timed step, threaded oracle "
-                                   "(CPU restatement of the reference engine)" % (rates[0][1], args.workload)},
+                         "sample": sample + " (CPU restatement of the reference engine)"},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
+def serve_sample(args, dev, count):
+    """A bounded sample of the served stream: the first `count` requests of the Poisson
+    stream, with their particles generated before the clock starts (client-side data)."""
+    from tfg import configs
+    from tfg.serving import Request, Server, summarize
+    reqs = []
+    for r in configs.served_requests(count=count, seed=args.seed):
+        reqs.append(Request(len(reqs), r["t"] - 0.0, configs.request_workload(r), r["steps"]))
+    t_first = reqs[0].t_arrival
+    for r in reqs:
+        r.t_arrival -= t_first
+    srv = Server(budget_bytes=150 << 30, max_particles=args.serve_particles, quantum=args.quantum, device=dev,
+                 keep_results=False)
+    done = srv.run(reqs)
+    s = summarize(done)
+    s.update({"max_concurrent": srv.max_concurrent, "chunks": srv.chunks, "quantum": args.quantum,
+              "max_particles_in_flight": args.serve_particles, "budget_bytes": 150 << 30,
+              "sample": "first %d of the 10,000 requests (arrivals re-based to t=0)" % count})
+    return s
+
+
+def run_ensemble(args, rank, world, dev, dist):
+    import torch
+    from tfg import configs
+    from tfg.engine import Batch, Engine, setup_model
+    ws = configs.ensemble(count=args.sims, seed=rank)
+    n_tot = sum(w.n for w in ws)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    cache = {}
+
+    def make_batch():
+        b = Batch(2, 0, dev)
+        b.set_stream(stream.cuda_stream)
+        sims = []
+        for w in ws:
+            s = b.add_sim(w.desc(device=dev))
+            b._keep.extend(setup_model(s, w, pot_cache=cache))
+            sims.append(s)
+        return b, sims
+
+    b, sims = make_batch()
+    split = b.autotune()
+    b.step(args.warmup)
+    cnt0, _ = b.pair_signature()
+    pairs0 = int(cnt0.sum()) // 2
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev, clock_path("clocks_bench.csv")) as clk:
+        e0.record(stream)
+        b.step(args.steps, sync=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    b.sync()
+    if dist is not None:
+        dist.barrier()
+    t_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        tt = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    value = world * n_tot * args.steps / (t_ms * 1e-3)
+    step_ms = t_ms / args.steps
+    # phase split and pair-kernel time from a few eager steps after the timed region
+    phase = np.zeros(4)
+    for _ in range(5):
+        b.step(1)
+        phase += np.array(b.phase_ms())
+    phase /= 5
+    cnt1, _ = b.pair_signature()
+    pairs = 0.5 * (pairs0 + int(cnt1.sum()) // 2)
+    b.close()
+
+    # plain path: every simulation alone in its own engine, one after another
+    kp = args.plain_steps
+    plain_ps, plain_ms = 0.0, 0.0
+    for w in ws:
+        e = Engine(w.desc(device=dev))
+        keep = setup_model(e, w, pot_cache=cache)
+        e.set_stream(stream.cuda_stream)
+        e.autotune()
+        e.step(3)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        e.step(kp, sync=False)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        e.sync()
+        plain_ms += a0.elapsed_time(a1)
+        plain_ps += w.n * kp
+        e.close()
+        del keep
+    plain = {"value": world * plain_ps / (plain_ms * 1e-3), "unit": "particle-steps/s",
+             "ms_per_round": plain_ms / kp, "steps_per_sim": kp,
+             "how": "each simulation alone in its own engine (same kernels, CUDA graphs), one after another"}
+
+    # end to end: the whole job through the C ABI with host arrays
+    E = args.e2e_steps
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    host = [(pin(w.x), pin(w.type), pin(w.radius), pin(w.imass)) for w in ws]
+    outs = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b2 = Batch(2, 0, dev)
+    b2.set_stream(stream.cuda_stream)
+    sims2 = []
+    for w, (hx, ht, hr, hi) in zip(ws, host):
+        s = b2.add_sim(w.desc(device=dev))
+        keep = setup_model(s, w, pot_cache=cache)
+        b2._keep.extend(keep)
+        s.load(hx, type=ht, radius=hr, imass=hi)
+        sims2.append(s)
+    b2.step(E)
+    for s in sims2:
+        outs.append(s.download())
+    t_e2e = time.perf_counter() - t0
+    b2.close()
+    bi = n_tot * (12 + 4 + 4 + 4)
+    bo = n_tot * (12 + 12 + 12 + 12 + 4 + 4)
+    e2e = {"value": world * n_tot * E / t_e2e, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": bi / E, "d2h_bytes_per_step": bo / E, "steps": E,
+           "how": "Batch + tfg_batch_add_sim/load_particles for all %d simulations from host arrays, "
+                  "tfg_step(%d), tfg_batch_download of each (x, xrel, v, f, cell, density); model set-up "
+                  "(potential tables cached from the batched run) inside the timed region" % (len(ws), E)}
+
+    # roofline: the pair kernel against the FP32 peak, the step against HBM
+    fl_pair = pairs * (FLOPS["table"] + FLOPS["density"])
+    achieved = fl_pair / (phase[1] * 1e-3) / 1e12
+    peak = fp32_peak(dev)
+    hbm, hbm_src = hbm_peak()
+    bytes_alg = n_tot * WORKLOADS["ensemble"]["bytes_per_particle"]
+    roof = {"bound": "fp32", "kernel": "k_pair_tile (split %d)" % split, "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+            "peak_source": "measured live (tfg_probe_fp32_tflops, FFMA chains)",
+            "flops_per_launch": fl_pair, "pairs_per_step": pairs,
+            "flops_per_pair": FLOPS["table"] + FLOPS["density"], "kernel_ms": phase[1], "traffic": None,
+            "step_hbm": {"achieved_gbs": bytes_alg / (step_ms * 1e-3) / 1e9, "peak_gbs": hbm,
+                         "peak_source": hbm_src, "frac": bytes_alg / (step_ms * 1e-3) / 1e9 / hbm,
+                         "bytes_per_step": bytes_alg}}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        sample = ensemble_sample(ws, 16)
+        rate, steps, dt = cpu_rate_sims(sample, threads, 15.0, max_steps=40)
+        cpu = {"value": rate, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+               "sample": "16 of the %d simulations (every %dth, %d particles), %d-%d steps each on the threaded "
+                         "CPU restatement of the reference engine, %.1f s" % (
+                             len(ws), max(1, len(ws) // 16), sum(w.n for w in sample), min(steps), max(steps), dt)}
+    serving = serve_sample(args, dev, args.requests) if (rank == 0 and args.requests > 0) else None
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "ensemble", "description": WORKLOADS["ensemble"]["desc"], "sims": len(ws),
+                       "n_particles": n_tot, "l2": "working set larger than L2 (not flushed)",
+                       "parallelism": "replicas%d" % world, "pair_split": split, "graphs": True,
+                       "phase_ms_per_step": dict(zip(["bin", "pair", "bonded", "advance"], phase.round(5).tolist()))},
+            "plain_gpu": plain, "batched_over_plain": value / plain["value"],
+            "serving": serving,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
+            "gpu_launches": launches_per_step() * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def run_served(args, rank, world, dev, dist):
+    with ClockSampler(dev, clock_path("clocks_served.csv")) as clk:
+        s = serve_sample(args, dev, args.requests or 100)
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": s["achieved_particle_steps_per_s"], "unit": "particle-steps/s",
+            "n_gpus": world, "steps": s["chunks"], "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "served", "description": WORKLOADS["served"]["desc"]},
+            "serving": s, "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
+def run_single(args, rank, world, dev, dist):
+    import torch
+    from tfg.engine import Engine, setup_model
+    w = make_workload(args.workload, rank, args.n or None, args.relax)
+    eng = Engine(w.desc(device=dev))
+    keep = setup_model(eng, w)
+    # a dedicated (non-default) stream shared by the engine and the timing events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    eng.set_stream(stream.cuda_stream)
+    if w.relax_steps:
+        # relaxation with the reference's overdamped displacement clamp (untimed)
+        for t in range(w.max_type):
+            eng.set_type(t, 1, w.mass[t])
+        eng.step(w.relax_steps)
+        for t in range(w.max_type):
+            eng.set_type(t, w.dynamics[t], w.mass[t])
+    split = eng.autotune()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        eng.step(1, sync=False)
+    torch.cuda.synchronize()
+    cnt0, _ = eng.pair_signature()
+    pairs0 = int(cnt0.sum()) // 2
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    phase_tot = np.zeros(4)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev, clock_path("clocks_bench.csv")) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            eng.step(1, sync=False)
+            ev[k][1].record(stream)
+            phase_tot += np.array(eng.phase_ms())
+        torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    t_ms = sum(a.elapsed_time(b) for a, b in ev)
+    cnt1, _ = eng.pair_signature()
+    pairs1 = int(cnt1.sum()) // 2
+    if dist is not None:
+        tt = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    value = world * w.n * args.steps / (t_ms * 1e-3)
+
+    # end to end: load from host arrays, run --e2e-steps steps, download
+    E = args.e2e_steps
+    pin = lambda a: None if a is None else torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    hx, hv, ht, hr, hi, hs = (pin(a) for a in (w.x, w.v, w.type, w.radius, w.imass, w.species))
+    e2e_eng = Engine(w.desc(device=dev))
+    keep2 = setup_model(e2e_eng, w)
+    e2e_eng.set_stream(stream.cuda_stream)
+    e2e_eng.set_split(split)
+    ns = w.nr_species
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_eng.load(hx, v=hv, type=ht, radius=hr, imass=hi, species=hs)
+    e2e_eng.step(E)
+    e2e_eng.download()
+    t_e2e = time.perf_counter() - t0
+    bi = w.n * (12 + 12 + 4 + 4 + 4 + 4 * ns)
+    bo = w.n * (12 + 12 + 4 + 12 + 12 + 4 + 8 * ns)
+    e2e = {"value": world * w.n * E / t_e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": bi / E,
+           "d2h_bytes_per_step": bo / E, "steps": E,
+           "how": "tfg_load_particles from host arrays, tfg_step(%d), tfg_download" % E}
+
+    pairs = 0.5 * (pairs0 + pairs1)
+    fl_pair = pairs * pair_flops(w)
+    pair_ms_avg = phase_tot[1] / args.steps
+    achieved = fl_pair / (pair_ms_avg * 1e-3) / 1e12
+    peak = fp32_peak(dev)
+    step_ms = t_ms / args.steps
+    bytes_alg = w.n * WORKLOADS[args.workload]["bytes_per_particle"]
+    hbm, hbm_src = hbm_peak()
+    roof = {"bound": "fp32", "kernel": "k_pair_tile (split %d)" % split, "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+            "peak_source": "measured live (tfg_probe_fp32_tflops, FFMA chains)",
+            "flops_per_launch": fl_pair, "pairs_per_step": pairs, "flops_per_pair": pair_flops(w),
+            "kernel_ms": pair_ms_avg, "traffic": None,
+            "step_hbm": {"achieved_gbs": bytes_alg / (step_ms * 1e-3) / 1e9, "peak_gbs": hbm, "peak_source": hbm_src,
+                         "frac": bytes_alg / (step_ms * 1e-3) / 1e9 / hbm, "bytes_per_step": bytes_alg}}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, steps, dt = cpu_rate_sims([w], threads, 15.0, max_steps=100)
+        cpu = {"value": rate, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+               "sample": "%d steps of the %s workload (%d particles) on the threaded CPU restatement "
+                         "of the reference engine, %.1f s" % (steps[0], args.workload, w.n, dt)}
+    if rank == 0:
+        line = {
+            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"],
+                       "n_particles": w.n, "cells": list(w.cells), "l2": "flushed between timed steps (256 MiB write)",
+                       "parallelism": "replicas%d" % world, "pair_split": split,
+                       "phase_ms_per_step": dict(zip(["bin", "pair", "bonded", "advance"],
+                                                     (phase_tot / args.steps).round(5).tolist()))},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
+            "gpu_launches": launches_per_step(w.bonds is not None, w.angles is not None) * args.steps,
+        }
+        print(json.dumps(line), flush=True)
+    del keep, keep2
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="dpd_droplets", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="ensemble", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="tfg", choices=["tfg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=20)
-    ap.add_argument("--n", type=int, default=0, help="scale the workload to n particles (same density)")
+    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--n", type=int, default=0, help="scale a single-simulation workload to n particles")
     ap.add_argument("--relax", type=int, default=None, help="override the relaxation steps")
+    ap.add_argument("--sims", type=int, default=256, help="simulations in the ensemble")
+    ap.add_argument("--plain-steps", type=int, default=20, help="timed steps per simulation on the plain path")
+    ap.add_argument("--requests", type=int, default=100, help="served-stream sample size (0: skip)")
+    ap.add_argument("--serve-particles", type=int, default=4_000_000, help="particles in flight cap")
+    ap.add_argument("--quantum", type=int, default=50, help="largest chunk of steps between admissions")
+    ap.add_argument("--seed", type=int, default=4)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -217,136 +603,15 @@ def main():
     else:
         torch.cuda.set_device(0)
     dev = torch.cuda.current_device()
-
     sys.path.insert(0, ROOT)
     import __graft_entry__
     __graft_entry__.build()
-    import ctypes as C
-    from tfg import lib
-    from tfg.engine import Engine, setup_model
-
-    w = make_workload(args.workload, rank, args.n or None, args.relax)
-    eng = Engine(w.desc(device=dev))
-    keep = setup_model(eng, w)
-    # a dedicated (non-default) stream shared by the engine and the timing events
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    eng.set_stream(stream.cuda_stream)
-    if w.relax_steps:
-        # steepest-descent-like relaxation with the reference's displacement clamp (untimed)
-        for t in range(w.max_type):
-            eng.set_type(t, 1, w.mass[t])
-        eng.step(w.relax_steps)
-        for t in range(w.max_type):
-            eng.set_type(t, w.dynamics[t], w.mass[t])
-
-    split = eng.autotune()
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    for _ in range(args.warmup):
-        eng.step(1, sync=False)
-    torch.cuda.synchronize()
-    cnt0, _ = eng.pair_signature()
-    pairs0 = int(cnt0.sum()) // 2
-
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    pair_ms = 0.0
-    phase_tot = np.zeros(4)
-    if dist is not None:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(dev, os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/clocks_bench.csv") as clk:
-        for k in range(args.steps):
-            flush.zero_()
-            ev[k][0].record(stream)
-            eng.step(1, sync=False)
-            ev[k][1].record(stream)
-            ph = eng.phase_ms()
-            phase_tot += np.array(ph)
-        torch.cuda.synchronize()
-    if dist is not None:
-        dist.barrier()
-    t_ms = sum(a.elapsed_time(b) for a, b in ev)
-    cnt1, _ = eng.pair_signature()
-    pairs1 = int(cnt1.sum()) // 2
-    if dist is not None:
-        tt = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms = float(tt.item())
-    value = world * w.n * args.steps / (t_ms * 1e-3)
-
-    # ---- end-to-end through the C ABI with host buffers
-    e2e = None
-    out = eng.download()
-    cell, xrel = out["cell"], out["xrel"]
-    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
-    h_cell, h_xrel, h_v = pin(cell), pin(xrel), pin(out["v"])
-    h_type, h_rad, h_im = pin(w.type), pin(w.radius), pin(w.imass)
-    h_sp = pin(out["species"]) if w.nr_species else None
-    e2e_eng = Engine(w.desc(device=dev))
-    keep2 = setup_model(e2e_eng, w)
-    ns = w.nr_species
-    bi = w.n * (4 + 12 + 12 + 4 + 4 + 4 + 4 * ns)
-    bo = w.n * (12 + 12 + 4 + 4 * ns)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for k in range(args.e2e_steps):
-        e2e_eng.load_binned(h_cell, h_xrel, v=h_v, type=h_type, radius=h_rad, imass=h_im, species=h_sp)
-        e2e_eng.step(1, sync=True)
-        o = e2e_eng.download()
-        h_cell, h_xrel, h_v = o["cell"], o["xrel"], o["v"]
-        if ns:
-            h_sp = o["species"]
-    t_e2e = time.perf_counter() - t0
-    e2e = {"value": w.n * args.e2e_steps / t_e2e * world, "unit": "particle-steps/s",
-           "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo, "steps": args.e2e_steps}
-
-    # ---- roofline of the pair kernel
-    pairs = 0.5 * (pairs0 + pairs1)
-    fl_pair = pairs * pair_flops(w)
-    pair_ms_avg = phase_tot[1] / args.steps
-    achieved = fl_pair / (pair_ms_avg * 1e-3) / 1e12
-    peak = C.c_double(0.0)
-    lib().tfg_probe_fp32_tflops(dev, C.byref(peak))
-    step_ms = t_ms / args.steps
-    bytes_alg = w.n * WORKLOADS[args.workload]["bytes_per_particle"]
-    hbm = None
-    try:
-        hbm = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
-    except Exception:
-        hbm = 6800.0
-    roof = {"bound": "fp32", "kernel": "k_pair_tile (split %d)" % split, "achieved": achieved, "peak": peak.value,
-            "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
-            "peak_source": "measured live (tfg_probe_fp32_tflops, FFMA chains)",
-            "flops_per_launch": fl_pair, "pairs_per_step": pairs, "flops_per_pair": pair_flops(w),
-            "kernel_ms": pair_ms_avg, "traffic": None,
-            "step_hbm": {"achieved_gbs": bytes_alg / (step_ms * 1e-3) / 1e9, "peak_gbs": hbm,
-                         "frac": bytes_alg / (step_ms * 1e-3) / 1e9 / hbm, "bytes_per_step": bytes_alg}}
-
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        rate, steps, dt = cpu_reference_rate(w, threads, 15.0, max_steps=100)
-        cpu = {"value": rate, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-               "sample": "%d steps of the %s workload (%d particles) on the threaded CPU restatement "
-                         "of the reference engine, %.1f s" % (steps, args.workload, w.n, dt)}
-
-    launches_per_step = 9 + (1 if w.bonds is not None else 0) + (1 if w.angles is not None else 0)
-    if rank == 0:
-        line = {
-            "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"],
-                       "n_particles": w.n, "cells": list(w.cells), "l2": "flushed between timed steps (256 MiB write)",
-                       "parallelism": "replicas%d" % world, "pair_split": split,
-                       "phase_ms_per_step": dict(zip(["bin", "pair", "bonded", "advance"],
-                                                     (phase_tot / args.steps).round(5).tolist()))},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
-            "gpu_launches": launches_per_step * args.steps,
-        }
-        print(json.dumps(line), flush=True)
-    del keep, keep2
+    if args.workload == "ensemble":
+        run_ensemble(args, rank, world, dev, dist)
+    elif args.workload == "served":
+        run_served(args, rank, world, dev, dist)
+    else:
+        run_single(args, rank, world, dev, dist)
     if dist is not None:
         dist.destroy_process_group()
 

@@ -228,6 +228,12 @@ TFG_API int tfg_step(tfg_engine *eng, int nsteps);
  * forces, without the advance.  Leaves f, number density and flux increments readable. */
 TFG_API int tfg_force_only(tfg_engine *eng, int with_bonded);
 TFG_API int tfg_sync(tfg_engine *eng);
+/* *idle = 1 when the engine's stream has no unfinished work, else 0 (never blocks). */
+TFG_API int tfg_query(tfg_engine *eng, int *idle);
+/* Replay steps from CUDA graphs (default on): tfg_step runs its first step eagerly, the
+ * middle ones as captured two-step graphs and the last eagerly (with phase events).  A
+ * graph is captured again after any change of layout, tables, work split or stream. */
+TFG_API int tfg_set_graphs(tfg_engine *eng, int enable);
 /* Autotune the nonbonded pass's work split (warps per home cell: 1, 2, 7 or 14) by timing
  * each choice on the current state; the state is left unchanged.  tfg_step and
  * tfg_force_only run it on their first call; tfg_set_split fixes the split instead.

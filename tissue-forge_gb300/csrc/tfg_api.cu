@@ -258,6 +258,7 @@ TFG_API int tfg_engine_set_stream(tfg_engine *eng, void *stream) {
         cudaStreamCreateWithFlags(&eng->stream, cudaStreamNonBlocking);
         eng->own_stream = true;
     }
+    eng->gen++;
     return TFG_OK;
 }
 
@@ -355,6 +356,7 @@ TFG_API int tfg_autotune(tfg_engine *eng, int *split) {
 TFG_API int tfg_set_split(tfg_engine *eng, int split) {
     if (!eng || !(split == 1 || split == 2 || split == 7 || split == 14)) return TFG_E_INVAL;
     eng->split = split;
+    eng->gen++;
     return TFG_OK;
 }
 
@@ -364,10 +366,24 @@ TFG_API int tfg_step(tfg_engine *eng, int nsteps) {
     int rc = commit(eng);
     if (rc) return rc;
     if (eng->split == 0 && (rc = autotune(eng))) return rc;
-    for (int k = 0; k < nsteps; k++) {
-        rc = one_step(eng, true, k == nsteps - 1);
-        if (rc) return rc;
+    return run_steps(eng, nsteps);
+}
+
+TFG_API int tfg_set_graphs(tfg_engine *eng, int enable) {
+    if (!eng) return TFG_E_INVAL;
+    eng->use_graphs = enable != 0;
+    return TFG_OK;
+}
+
+TFG_API int tfg_query(tfg_engine *eng, int *idle) {
+    if (!eng || !idle) return TFG_E_INVAL;
+    cudaError_t e = cudaStreamQuery(eng->stream);
+    if (e == cudaErrorNotReady) {
+        *idle = 0;
+        return TFG_OK;
     }
+    if (e != cudaSuccess) return fail(eng, TFG_E_CUDA, cudaGetErrorString(e));
+    *idle = 1;
     return TFG_OK;
 }
 

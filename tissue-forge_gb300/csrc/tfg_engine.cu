@@ -535,6 +535,7 @@ int bin(tfg_engine *eng, int shuffle) {
 int commit(tfg_engine *eng) {
     int rc;
     const bool relaid = eng->layout_dirty;
+    if (eng->layout_dirty || eng->tables_dirty) eng->gen++;
     if (eng->layout_dirty && (rc = relayout(eng))) return rc;
     if (eng->tables_dirty && (rc = upload_tables(eng))) return rc;
     if (relaid) {
@@ -603,9 +604,8 @@ int force_pass(tfg_engine *eng, bool bonded, bool timed) {
     return check_launch(eng);
 }
 
-int one_step(tfg_engine *eng, bool advance, bool timed) {
+int enqueue_step(tfg_engine *eng, bool advance, bool timed) {
     cudaStream_t s = eng->stream;
-    for (int k : eng->order) eng->sims[k].time += 1;
     const int nsims = (int)eng->order.size();
     launch_tick(nsims, eng->sims_dev, s);
     CK(cudaMemsetAsync(eng->red, 0, sizeof(double) * std::max(nsims, 1) * RED_COUNT, s));
@@ -620,6 +620,63 @@ int one_step(tfg_engine *eng, bool advance, bool timed) {
                        eng->type_mass, eng->type_dyn, eng->species_flags, eng->red, eng->err, s);
     if (timed) cudaEventRecord(eng->ev[4], s);
     return check_launch(eng);
+}
+
+int one_step(tfg_engine *eng, bool advance, bool timed) {
+    for (int k : eng->order) eng->sims[k].time += 1;
+    return enqueue_step(eng, advance, timed);
+}
+
+void drop_graphs(tfg_engine *eng) {
+    for (int p = 0; p < 2; p++) {
+        if (eng->graph[p]) cudaGraphExecDestroy(eng->graph[p]);
+        eng->graph[p] = nullptr;
+        eng->graph_gen[p] = 0;
+    }
+}
+
+int graph_step_pair(tfg_engine *eng) {
+    const int p = eng->cur;
+    if (!eng->graph[p] || eng->graph_gen[p] != eng->gen) {
+        if (eng->graph[p]) cudaGraphExecDestroy(eng->graph[p]);
+        eng->graph[p] = nullptr;
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(eng->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_step(eng, true, false);
+        if (!rc) rc = enqueue_step(eng, true, false);
+        cudaError_t e = cudaStreamEndCapture(eng->stream, &g);
+        eng->cur = p;  // two buffer swaps: the host view is where it started
+        if (rc || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            return rc ? rc : fail(eng, TFG_E_CUDA, std::string("step capture: ") + cudaGetErrorString(e));
+        }
+        e = cudaGraphInstantiate(&eng->graph[p], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            eng->graph[p] = nullptr;
+            return fail(eng, TFG_E_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+        }
+        eng->graph_gen[p] = eng->gen;
+    }
+    CK(cudaGraphLaunch(eng->graph[p], eng->stream));
+    for (int k : eng->order) eng->sims[k].time += 2;
+    return TFG_OK;
+}
+
+int run_steps(tfg_engine *eng, int nsteps) {
+    // All but the last step in captured pairs (after one eager step has configured every
+    // kernel), the last eagerly with phase events.
+    int k = 0, rc;
+    if (eng->use_graphs && nsteps >= 4) {
+        if ((rc = one_step(eng, true, false))) return rc;
+        k = 1;
+        for (; k + 2 < nsteps; k += 2)
+            if ((rc = graph_step_pair(eng))) return rc;
+    }
+    for (; k < nsteps; k++)
+        if ((rc = one_step(eng, true, k == nsteps - 1))) return rc;
+    return TFG_OK;
 }
 
 // Pick the tiled pair kernel's work split (warps per home cell) by timing each choice on
@@ -663,6 +720,7 @@ int autotune(tfg_engine *eng) {
     if (rc) return rc;
     CK(cudaStreamSynchronize(s));
     eng->split = best_split;
+    eng->gen++;
     return check_launch(eng);
 }
 
@@ -670,7 +728,9 @@ int download_sim(tfg_engine *eng, int sim, float *x, float *xrel, int32_t *cell,
                  float *species, float *q) {
     int rc = sim_check(eng, sim);
     if (rc) return rc;
-    if ((rc = commit(eng))) return rc;
+    // A simulation already in the arena is read where it lies, without re-laying the arena
+    // out for other simulations' pending changes.
+    if ((!eng->sims[sim].in_arena || eng->sims[sim].pending) && (rc = commit(eng))) return rc;
     SimHost &S = eng->sims[sim];
     const int n = S.n, ns = eng->nspec;
     if (n == 0) return TFG_OK;
@@ -709,7 +769,7 @@ int reductions_sim(tfg_engine *eng, int sim, tfg_reductions *out) {
     std::memset(out, 0, sizeof(*out));
     SimHost &S = eng->sims[sim];
     out->steps = S.time;
-    if (!S.in_arena || eng->layout_dirty) return TFG_OK;
+    if (!S.in_arena) return TFG_OK;
     double r[RED_COUNT];
     CK(cudaMemcpyAsync(r, eng->red + S.P.red_base, sizeof(r), cudaMemcpyDeviceToHost, eng->stream));
     CK(cudaStreamSynchronize(eng->stream));
@@ -727,6 +787,7 @@ int reductions_sim(tfg_engine *eng, int sim, tfg_reductions *out) {
 
 void destroy(tfg_engine *eng) {
     if (eng->stream) cudaStreamSynchronize(eng->stream);
+    drop_graphs(eng);
     for (int b = 0; b < 2; b++) free_particles(eng->A[b]);
     void *bufs[] = {eng->force, eng->count, eng->start, eng->lidx, eng->tmp_id, eng->tmp_src, eng->dest,
                     eng->slot_of_id, eng->scan_sums, eng->cell_sim, eng->overflow_list, eng->overflow_count,

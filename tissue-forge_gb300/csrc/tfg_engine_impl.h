@@ -92,6 +92,14 @@ struct tfg_engine {
     uint32_t flags_all = 0;          // TFG_ENGINE_NO_DENSITY only when every simulation sets it
     int split = 0;                   // tiled pair pass: warps per home cell (0 = not tuned)
     int capacity_hint = 0;
+    // CUDA graphs of two consecutive steps, one per starting buffer parity (a step swaps
+    // the particle buffers, so two steps return to the parity they started from).  `gen`
+    // changes whenever a captured launch argument may have changed (layout, tables, split,
+    // stream); a graph captured under another generation is captured again.
+    bool use_graphs = true;
+    uint64_t gen = 1;
+    uint64_t graph_gen[2] = {0, 0};
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
 };
 
 namespace tfg {
@@ -117,6 +125,9 @@ int commit(tfg_engine *eng);                    // re-lay the arena out and uplo
 int bin(tfg_engine *eng, int shuffle);
 int force_pass(tfg_engine *eng, bool bonded, bool timed);
 int one_step(tfg_engine *eng, bool advance, bool timed);
+int enqueue_step(tfg_engine *eng, bool advance, bool timed);  // one_step without the host clock
+int graph_step_pair(tfg_engine *eng);           // two steps replayed from a captured graph
+int run_steps(tfg_engine *eng, int nsteps);     // nsteps steps, graphs where they apply
 int autotune(tfg_engine *eng);
 PairKernelArgs pair_args(tfg_engine *eng);
 bool use_tile(const tfg_engine *eng);

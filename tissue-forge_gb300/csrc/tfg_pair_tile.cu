@@ -35,7 +35,7 @@ struct Staged {
     float4 pos[kCapT];      // cell-relative position; w = type bits
     float4 acc[kCapT];      // fx, fy, fz, number density (signature: count, hash bits)
     int32_t gslot[kCapT];   // global slot of the staged particle
-    float4 sh4[kCapT];      // shift of the staged particle's cell as seen from the home cell
+    float4 sh4[kCapT];      // shift of the staged particle's cell as seen from the home cell; w = radius
     float sh[27][3];        // shift of each task's partner cell (space_getsid)
     uint32_t q[kQ];         // packed hit (i | k << 16), staged indices
 };
@@ -104,12 +104,8 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
     const PotDev &pot = pots[pidx];
     if (pot.kind == POT_TABLE) {
         float e, f;
-        float ri = 0.f, rk = 0.f;
-        if (pot.flags & (TFG_POTENTIAL_SHIFTED | TFG_POTENTIAL_SCALED)) {
-            ri = a.aux[gi].x;
-            rk = a.aux[gk].x;
-        }
-        if (table_eval(pot, blob, ri, rk, r2, e, f)) {
+        // radii ride in the staged shift's w component
+        if (table_eval(pot, blob, S.sh4[I].w, s4.w, r2, e, f)) {
             const float wx = f * dx.x, wy = f * dx.y, wz = f * dx.z;
             fI.x -= wx; fI.y -= wy; fI.z -= wz;
             fK.x += wx; fK.y += wy; fK.z += wz;
@@ -228,12 +224,11 @@ __device__ __forceinline__ void flush_red(double *red, int rb, float &epot, floa
 template <bool kFlux, bool kSig>
 __device__ __forceinline__ void stage(const PairKernelArgs &a, Staged &S, float *SQ, int base, int g0, int n,
                                       int task, int lane) {
-    const float4 sh = make_float4(S.sh[task][0], S.sh[task][1], S.sh[task][2], 0.f);
     for (int k = lane; k < n; k += 32) {
         S.pos[base + k] = a.pos[g0 + k];
         S.acc[base + k] = make_float4(0.f, 0.f, 0.f, 0.f);
         S.gslot[base + k] = g0 + k;
-        S.sh4[base + k] = sh;
+        S.sh4[base + k] = make_float4(S.sh[task][0], S.sh[task][1], S.sh[task][2], a.aux[g0 + k].x);
         if (!kSig && kFlux) SQ[base + k] = 0.f;
     }
 }
@@ -318,6 +313,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
             S.sh[d][2] = cell_shift(P, 2, lk, mk);
         }
         if (lane == 13) { S.sh[13][0] = 0.f; S.sh[13][1] = 0.f; S.sh[13][2] = 0.f; }
+        __syncwarp();
         // capacity: every group of this home cell takes the same decision
         const bool over = nh > kHomeCap || (lane < 13 && nh + my_n > kCapT);
         if (__any_sync(0xffffffffu, over)) {

@@ -48,6 +48,8 @@ def lib():
     L.tfg_step.argtypes = [E, C.c_int]
     L.tfg_force_only.argtypes = [E, C.c_int]
     L.tfg_sync.argtypes = [E]
+    L.tfg_query.argtypes = [E, C.POINTER(C.c_int)]
+    L.tfg_set_graphs.argtypes = [E, C.c_int]
     L.tfg_pair_signature.argtypes = [E, abi.I_P, abi.U_P]
     L.tfg_autotune.argtypes = [E, C.POINTER(C.c_int)]
     L.tfg_set_split.argtypes = [E, C.c_int]

@@ -81,6 +81,14 @@ class Workload:
                                max_bonds=nb, max_angles=na, device=device, flags=self.flags)
 
 
+def in_box(x, side):
+    """Wrap positions into the periodic box [0, side) and keep them off its upper face:
+    space_setpartp (tfSpace.cpp:443-448) rejects a particle whose clamped coordinate
+    rounds to cell index cdim, which FP32 can do within a few ulps of the face."""
+    x = np.mod(np.asarray(x, np.float64), side)
+    return np.minimum(x, side * (1.0 - 1e-6)).astype(np.float32)
+
+
 def cells_for(side, cutoff):
     """Cells per axis with edge >= cutoff (span 1): floor(side/cutoff), at least 3."""
     return max(3, int(math.floor(side / cutoff)))
@@ -88,7 +96,7 @@ def cells_for(side, cutoff):
 
 def cell_sorting(n=4000, side=20.0, cutoff=3.0, depth_ab=0.5, steps=100, seed=0, random_force=None):
     rng = np.random.default_rng(np.random.PCG64(seed))
-    x = rng.uniform(0.0, side, size=(n, 3)).astype(np.float32)
+    x = in_box(rng.uniform(0.0, side, size=(n, 3)), side)
     t = np.zeros(n, np.int32)
     t[rng.permutation(n)[: n // 2]] = 1
     c = cells_for(side, cutoff)
@@ -118,7 +126,7 @@ def dpd_droplets(n=100_000, side=40.0, cutoff=1.0, radius=12.0, steps=1000, seed
             got = np.concatenate([got, cand])
         pts.append(got[:m] + centres[d])
         drop.append(np.full(m, d, np.int32))
-    x = np.concatenate(pts).astype(np.float32)
+    x = in_box(np.concatenate(pts), side)
     droplet = np.concatenate(drop)
     v = rng.normal(0.0, 1.0, size=(n, 3)).astype(np.float32)   # kT = 1, m = 1
     species = droplet.astype(np.float32).reshape(n, 1)          # 0 in droplet 1, 1 in droplet 2
@@ -152,7 +160,7 @@ def bonded_fluid(n=2_000_000, density=0.85, cutoff=2.5, chain=16, steps=500, rel
     dirs = rng.normal(size=(nch, chain - 1, 3))
     dirs /= np.linalg.norm(dirs, axis=2, keepdims=True)
     walk = np.concatenate([np.zeros((nch, 1, 3)), np.cumsum(dirs, axis=1)], axis=1) + starts[:, None, :]
-    x = np.mod(walk.reshape(n, 3), side).astype(np.float32)
+    x = in_box(walk.reshape(n, 3), side)
     ids = np.arange(n, dtype=np.int32).reshape(nch, chain)
     bonds = np.stack([ids[:, :-1].reshape(-1), ids[:, 1:].reshape(-1)], axis=1).astype(np.int32)
     angles = np.stack([ids[:, :-2].reshape(-1), ids[:, 1:-1].reshape(-1), ids[:, 2:].reshape(-1)],

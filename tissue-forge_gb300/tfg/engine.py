@@ -147,6 +147,15 @@ class Engine:
     def sync(self):
         self._chk(self.L.tfg_sync(self.h), "sync")
 
+    def idle(self):
+        """True when the engine's stream has finished all queued work (does not block)."""
+        v = C.c_int()
+        self._chk(self.L.tfg_query(self.h, C.byref(v)), "query")
+        return bool(v.value)
+
+    def set_graphs(self, enable):
+        self._chk(self.L.tfg_set_graphs(self.h, 1 if enable else 0), "set_graphs")
+
     def download(self):
         n, ns = self.n, self.nspec
         out = dict(x=np.zeros((n, 3), np.float32), xrel=np.zeros((n, 3), np.float32),
@@ -305,15 +314,26 @@ class Sim:
         return r
 
 
-def setup_model(eng, w, keep=None):
+def _potential(spec, cache):
+    if cache is None:
+        return Potential.from_spec(spec)
+    key = (spec.kind, tuple(sorted(spec.args.items())))
+    p = cache.get(key)
+    if p is None:
+        p = cache[key] = Potential.from_spec(spec)
+    return p
+
+
+def setup_model(eng, w, keep=None, pot_cache=None):
     """Apply a configs.Workload's interaction model and particles to an engine-like object
-    (the GPU Engine or the CPU oracle share these method names).  Returns the Potential
-    objects, which must stay alive while the engine uses their tables."""
+    (the GPU Engine, a batch Sim, or the CPU oracle share these method names).  Returns the
+    Potential objects, which must stay alive while the engine uses their tables.  With a
+    pot_cache dict, equal potential specifications share one table."""
     pots = []
     for t in range(w.max_type):
         eng.set_type(t, w.dynamics[t], w.mass[t])
     for (ti, tj), spec in w.pots.items():
-        p = Potential.from_spec(spec)
+        p = _potential(spec, pot_cache)
         pots.append(p)
         eng.set_potential(ti, tj, p.ptr)
     for (ti, tj, f) in w.fluxes:
@@ -323,11 +343,11 @@ def setup_model(eng, w, keep=None):
         for t in range(w.max_type):
             eng.set_random_force(t, mean, std, dur)
     if w.bond_pot is not None:
-        p = Potential.from_spec(w.bond_pot)
+        p = _potential(w.bond_pot, pot_cache)
         pots.append(p)
         eng.set_bonded_potential(0, p.ptr)
     if w.angle_pot is not None:
-        p = Potential.from_spec(w.angle_pot)
+        p = _potential(w.angle_pot, pot_cache)
         pots.append(p)
         eng.set_bonded_potential(1, p.ptr)
     eng.load(w.x, v=w.v, type=w.type, radius=w.radius, imass=w.imass, species=w.species)
