@@ -297,7 +297,10 @@ def run_ensemble(args, rank, world, dev, dist):
     import torch
     from tfg import configs
     from tfg.engine import Batch, Engine, setup_model
-    ws = configs.ensemble(count=args.sims, seed=rank)
+    from tfg.sharding import max_over_ranks, shard
+    # an ensemble of sims x world simulations, LPT-partitioned over the ranks by work
+    ns_all, _ = configs.ensemble_sizes(args.sims * world)
+    ws = configs.ensemble(count=args.sims * world, indices=shard(ns_all, rank, world))
     n_tot = sum(w.n for w in ws)
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -330,12 +333,9 @@ def run_ensemble(args, rank, world, dev, dist):
     b.sync()
     if dist is not None:
         dist.barrier()
-    t_ms = e0.elapsed_time(e1)
-    if dist is not None:
-        tt = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms = float(tt.item())
-    value = world * n_tot * args.steps / (t_ms * 1e-3)
+    t_ms = max_over_ranks(e0.elapsed_time(e1), dist, device="cuda")
+    n_all = int(np.sum(ns_all))
+    value = n_all * args.steps / (t_ms * 1e-3)
     step_ms = t_ms / args.steps
     # phase split and pair-kernel time from a few eager steps after the timed region
     phase = np.zeros(4)
@@ -366,7 +366,8 @@ def run_ensemble(args, rank, world, dev, dist):
         plain_ps += w.n * kp
         e.close()
         del keep
-    plain = {"value": world * plain_ps / (plain_ms * 1e-3), "unit": "particle-steps/s",
+    plain_ms = max_over_ranks(plain_ms, dist, device="cuda")
+    plain = {"value": n_all * kp / (plain_ms * 1e-3), "unit": "particle-steps/s",
              "ms_per_round": plain_ms / kp, "steps_per_sim": kp,
              "how": "each simulation alone in its own engine (same kernels, CUDA graphs), one after another"}
 
@@ -393,7 +394,8 @@ def run_ensemble(args, rank, world, dev, dist):
     b2.close()
     bi = n_tot * (12 + 4 + 4 + 4)
     bo = n_tot * (12 + 12 + 12 + 12 + 4 + 4)
-    e2e = {"value": world * n_tot * E / t_e2e, "unit": "particle-steps/s",
+    t_e2e = max_over_ranks(t_e2e, dist, device="cuda")
+    e2e = {"value": n_all * E / t_e2e, "unit": "particle-steps/s",
            "h2d_bytes_per_step": bi / E, "d2h_bytes_per_step": bo / E, "steps": E,
            "how": "Batch + tfg_batch_add_sim/load_particles for all %d simulations from host arrays, "
                   "tfg_step(%d), tfg_batch_download of each (x, xrel, v, f, cell, density); model set-up "
@@ -430,7 +432,8 @@ def run_ensemble(args, rank, world, dev, dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "ensemble", "description": WORKLOADS["ensemble"]["desc"], "sims": len(ws),
-                       "n_particles": n_tot, "l2": "working set larger than L2 (not flushed)",
+                       "n_particles": n_tot, "sims_all_ranks": args.sims * world, "n_particles_all_ranks": n_all,
+                       "sharding": "LPT over ranks by particle count, no data-path collective", "l2": "working set larger than L2 (not flushed)",
                        "parallelism": "replicas%d" % world, "pair_split": split, "graphs": True,
                        "phase_ms_per_step": dict(zip(["bin", "pair", "bonded", "advance"], phase.round(5).tolist()))},
             "plain_gpu": plain, "batched_over_plain": value / plain["value"],

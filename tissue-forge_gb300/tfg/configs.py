@@ -177,13 +177,20 @@ def bonded_fluid(n=2_000_000, density=0.85, cutoff=2.5, chain=16, steps=500, rel
     return w
 
 
-def ensemble(count=256, nmin=500, nmax=50_000, density=0.5, cutoff=3.0, steps=1000, seed=3):
-    """Parameter sweep: `count` independent cell_sorting-style simulations."""
+def ensemble_sizes(count=256, nmin=500, nmax=50_000, seed=3):
+    """Particle counts and A-B depths of the parameter sweep (no particle data)."""
     rng = np.random.default_rng(np.random.PCG64(3000 + seed))
     ns = np.exp(rng.uniform(math.log(nmin), math.log(nmax), size=count)).astype(np.int64)
     depths = rng.uniform(0.1, 2.0, size=count)
+    return ns, depths
+
+
+def ensemble(count=256, nmin=500, nmax=50_000, density=0.5, cutoff=3.0, steps=1000, seed=3, indices=None):
+    """Parameter sweep: `count` independent cell_sorting-style simulations (or only those
+    listed in `indices`; each simulation depends only on its index and `seed`)."""
+    ns, depths = ensemble_sizes(count, nmin, nmax, seed)
     sims = []
-    for i in range(count):
+    for i in (range(count) if indices is None else indices):
         n = int(ns[i])
         side = float((n / density) ** (1.0 / 3.0))
         w = cell_sorting(n=n, side=side, cutoff=cutoff, depth_ab=float(depths[i]), steps=steps,
