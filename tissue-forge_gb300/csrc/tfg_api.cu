@@ -419,7 +419,8 @@ TFG_API int tfg_pair_signature(tfg_engine *eng, int32_t *count, uint32_t *hash) 
     a.sig_hash = reinterpret_cast<uint32_t *>(dbuf + n);
     cudaMemsetAsync(dbuf, 0, sizeof(int32_t) * 2 * n, eng->stream);
     if (use_tile(eng))
-        launch_pair_tile(a, eng->overflow_list, eng->overflow_count, eng->sms, true, eng->split, eng->stream);
+        launch_pair_tile(a, tile_plan(eng, eng->split), eng->overflow_list, eng->overflow_count, eng->sms, true,
+                         eng->split, eng->stream);
     else
         launch_pair_signature(a, eng->stream);
     cudaMemcpyAsync(count, a.sig_count, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, eng->stream);

@@ -34,15 +34,18 @@ enum : uint32_t {
 enum : uint32_t { STREAM_DPD = 0xD0D0u, STREAM_FORCE = 0xF0F0u, STREAM_ANGLE = 0xA0A0u };
 
 // One potential as consumed by the kernels (struct Potential, tfPotential.h:213-253).
-struct PotDev {
+// 64 bytes, 16-byte aligned: a descriptor is read with four 128-bit loads.
+struct __align__(16) PotDev {
     uint32_t kind;       // 0 none, 1 table, 2 dpd  (internal encoding, see engine)
     uint32_t flags;
     float alpha0, alpha1, alpha2;
     float r0_plusone, a, b;
     int32_t n;
-    int32_t offset;      // float offset of the table in the table blob
+    int32_t offset;      // float offset of the table in the table blob (a multiple of 8)
     float dpd_alpha, dpd_gamma, dpd_sigma;
+    float pad_[3];
 };
+static_assert(sizeof(PotDev) == 64, "PotDev layout");
 enum : uint32_t { POT_NONE = 0, POT_TABLE = 1, POT_DPD = 2 };
 
 struct FluxDev {
@@ -165,6 +168,26 @@ __device__ __forceinline__ float density_w(float r, float inv_h, float norm) {
     return y * norm;   // norm = 1 / (pi h^3)
 }
 
+// One interval of a table (potential_eval_ex's polynomial, tf_potential_eval.h:128-139):
+// x = (r - c0) c1, ee and eff by the Horner recurrence over c2..c7.  The row is 8 floats,
+// 32-byte aligned (table offsets are multiples of 8), read as two 128-bit loads.
+__device__ __forceinline__ void table_row_eval(const float *row, float r, float &ee, float &eff, float &c1) {
+    const float4 *c4 = reinterpret_cast<const float4 *>(row);
+    const float4 ca = c4[0], cb = c4[1];
+    const float x = (r - ca.x) * ca.y;
+    ee = fmaf(ca.z, x, ca.w);
+    eff = ca.z;
+    eff = fmaf(eff, x, ee);
+    ee = fmaf(ee, x, cb.x);
+    eff = fmaf(eff, x, ee);
+    ee = fmaf(ee, x, cb.y);
+    eff = fmaf(eff, x, ee);
+    ee = fmaf(ee, x, cb.z);
+    eff = fmaf(eff, x, ee);
+    ee = fmaf(ee, x, cb.w);
+    c1 = ca.y;
+}
+
 // Tabulated potential (potential_eval_ex, tf_potential_eval.h:104-146).  Returns false
 // when out of range.  The interval index is computed with the reference's unfused FP32
 // arithmetic so the same interval is chosen; the Horner recurrence uses FMA.
@@ -178,16 +201,10 @@ __device__ __forceinline__ bool table_eval(const PotDev &p, const float *__restr
     float t = __fadd_rn(p.alpha0, __fmul_rn(r, __fadd_rn(p.alpha1, __fmul_rn(r, p.alpha2))));
     unsigned ind = (unsigned)fmaxf(0.0f, t);
     if (r > p.b || ind > (unsigned)p.n) return false;
-    const float *c = blob + p.offset + ind * kChunk;
-    float x = (r - c[0]) * c[1];
-    float ee = fmaf(c[2], x, c[3]), eff = c[2];
-#pragma unroll
-    for (int k = 4; k < kChunk; k++) {
-        eff = fmaf(eff, x, ee);
-        ee = fmaf(ee, x, c[k]);
-    }
+    float ee, eff, c1;
+    table_row_eval(blob + p.offset + ind * kChunk, r, ee, eff, c1);
     e = ee;
-    f = __fdiv_rn(eff * c[1], ro);
+    f = __fdiv_rn(eff * c1, ro);
     return true;
 }
 

@@ -301,8 +301,17 @@ int upload_tables(tfg_engine *eng) {
         for (int k = 0; k < T * T; k++) {
             PotDev d = S.pots[k];
             if (d.kind == POT_TABLE) {
-                d.offset = (int)blob.size();
-                blob.insert(blob.end(), S.tables[k].begin(), S.tables[k].end());
+                // a table equal to an earlier one of the same simulation (the (j,i) copy of
+                // (i,j), or a shared potential) is stored once
+                int found = -1;
+                for (int k2 = 0; k2 < k && found < 0; k2++)
+                    if (S.pots[k2].kind == POT_TABLE && S.tables[k2] == S.tables[k]) found = pots[q * T * T + k2].offset;
+                if (found >= 0) {
+                    d.offset = found;
+                } else {
+                    d.offset = (int)blob.size();
+                    blob.insert(blob.end(), S.tables[k].begin(), S.tables[k].end());
+                }
             }
             if (d.kind == POT_DPD) eng->has_dpd = true;
             if (S.fluxes[k].count > 0) eng->has_flux = true;
@@ -582,6 +591,15 @@ PairKernelArgs pair_args(tfg_engine *eng) {
     return a;
 }
 
+const TilePlan &tile_plan(tfg_engine *eng, int split) {
+    if (eng->plan_gen != eng->gen || eng->plan_split != split) {
+        eng->plan = plan_pair_tile((int)eng->order.size(), eng->max_type, eng->blob_floats);
+        eng->plan_gen = eng->gen;
+        eng->plan_split = split;
+    }
+    return eng->plan;
+}
+
 // The tiled half-shell kernel handles at most one species; more go to the stencil kernel.
 bool use_tile(const tfg_engine *eng) { return !(eng->has_flux && eng->nspec > 1); }
 
@@ -590,7 +608,9 @@ int force_pass(tfg_engine *eng, bool bonded, bool timed) {
     ParticleArrays &A = eng->A[eng->cur];
     PairKernelArgs a = pair_args(eng);
     if (eng->n > 0) {
-        if (use_tile(eng)) launch_pair_tile(a, eng->overflow_list, eng->overflow_count, eng->sms, false, eng->split, s);
+        if (use_tile(eng))
+            launch_pair_tile(a, tile_plan(eng, eng->split), eng->overflow_list, eng->overflow_count, eng->sms, false,
+                             eng->split, s);
         else launch_pair(a, s);
     }
     if (timed) cudaEventRecord(eng->ev[2], s);
@@ -704,7 +724,8 @@ int autotune(tfg_engine *eng) {
             if (rc) { cudaFree(save); return rc; }
             PairKernelArgs a = pair_args(eng);
             cudaEventRecord(eng->ev[0], s);
-            launch_pair_tile(a, eng->overflow_list, eng->overflow_count, eng->sms, false, cand[c], s);
+            launch_pair_tile(a, tile_plan(eng, cand[c]), eng->overflow_list, eng->overflow_count, eng->sms, false,
+                             cand[c], s);
             cudaEventRecord(eng->ev[1], s);
             CK(cudaEventSynchronize(eng->ev[1]));
             float ms = 0.f;

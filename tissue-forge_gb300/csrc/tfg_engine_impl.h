@@ -96,6 +96,10 @@ struct tfg_engine {
     // the particle buffers, so two steps return to the parity they started from).  `gen`
     // changes whenever a captured launch argument may have changed (layout, tables, split,
     // stream); a graph captured under another generation is captured again.
+    // tiled-pass staging plan, cached for (generation, split)
+    tfg::TilePlan plan;
+    uint64_t plan_gen = 0;
+    int plan_split = 0;
     bool use_graphs = true;
     uint64_t gen = 1;
     uint64_t graph_gen[2] = {0, 0};
@@ -130,6 +134,7 @@ int graph_step_pair(tfg_engine *eng);           // two steps replayed from a cap
 int run_steps(tfg_engine *eng, int nsteps);     // nsteps steps, graphs where they apply
 int autotune(tfg_engine *eng);
 PairKernelArgs pair_args(tfg_engine *eng);
+const TilePlan &tile_plan(tfg_engine *eng, int split);
 bool use_tile(const tfg_engine *eng);
 PotDev to_dev(const tfg_potential *p);
 int load_sim(tfg_engine *eng, int sim, int n, const float *xg, const int32_t *cellv, const float *xrel,

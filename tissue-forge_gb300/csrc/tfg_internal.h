@@ -78,8 +78,16 @@ void launch_pair(const PairKernelArgs &a, cudaStream_t s);
 // the initial force, to which both partners' contributions are added atomically.
 // `split` = warps per home cell (1, 2, 7 or 14): the cell's 14 tasks are divided into
 // that many work items.
-void launch_pair_tile(const PairKernelArgs &a, int *overflow_list, int *overflow_count, int sms, bool signature,
-                      int split, cudaStream_t s);
+// Shared-memory staging of the tiled pass: every potential table and descriptor of the
+// arena is staged per CTA when they fit (the usual case for one simulation), else none is
+// and they are read through L1.
+struct TilePlan {
+    int stage_floats = 0;
+    int stage_pots = 0;
+};
+TilePlan plan_pair_tile(int nsims, int max_type, int blob_floats);
+void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overflow_list, int *overflow_count, int sms,
+                      bool signature, int split, cudaStream_t s);
 int pair_tile_capacity();
 // Same stencil walk and pair decision as launch_pair, writing only the per-particle
 // pair signature (used to prove the pair set bit-exact against the oracle).

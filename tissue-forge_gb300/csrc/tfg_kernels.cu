@@ -304,15 +304,9 @@ __global__ void k_bonds(int nb, const SimParams *sims, const int32_t *cell_sim, 
                 const float t = __fadd_rn(pot.alpha0, __fmul_rn(rb_, __fadd_rn(pot.alpha1, __fmul_rn(rb_, pot.alpha2))));
                 int ind = (int)fmaxf(0.0f, t);
                 if (ind > pot.n) ind = pot.n;
-                const float *c = bblob + pot.offset + ind * kChunk;
-                const float x = (rb_ - c[0]) * c[1];
-                float ee = fmaf(c[2], x, c[3]), eff = c[2];
-#pragma unroll
-                for (int k = 4; k < kChunk; k++) {
-                    eff = fmaf(eff, x, ee);
-                    ee = fmaf(ee, x, c[k]);
-                }
-                const float f = eff * c[1] / rb_;
+                float ee, eff, c1;
+                table_row_eval(bblob + pot.offset + ind * kChunk, rb_, ee, eff, c1);
+                const float f = eff * c1 / rb_;
                 atomicAdd(&force[si], make_float4(-f * dx, -f * dy, -f * dz, 0.f));
                 atomicAdd(&force[sj], make_float4(f * dx, f * dy, f * dz, 0.f));
                 epot = ee;
@@ -383,15 +377,9 @@ __global__ void k_angles(int na, const SimParams *sims, const int32_t *cell_sim,
                 const float t = __fadd_rn(pot.alpha0, __fmul_rn(rr, __fadd_rn(pot.alpha1, __fmul_rn(rr, pot.alpha2))));
                 const int ind = (int)fmaxf(0.0f, t);
                 if (ind <= pot.n) {
-                    const float *c = bblob + pot.offset + ind * kChunk;
-                    const float x = (rr - c[0]) * c[1];
-                    float ee = fmaf(c[2], x, c[3]), eff = c[2];
-#pragma unroll
-                    for (int k = 4; k < kChunk; k++) {
-                        eff = fmaf(eff, x, ee);
-                        ee = fmaf(ee, x, c[k]);
-                    }
-                    eff = eff * c[1];
+                    float ee, eff, c1;
+                    table_row_eval(bblob + pot.offset + ind * kChunk, rr, ee, eff, c1);
+                    eff = eff * c1;
                     float wi[3], wk[3];
                     for (int k = 0; k < 3; k++) { wi[k] = eff * dxi[k]; wk[k] = eff * dxk[k]; }
                     atomicAdd(&force[si], make_float4(-wi[0], -wi[1], -wi[2], 0.f));

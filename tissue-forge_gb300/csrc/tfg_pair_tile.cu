@@ -53,6 +53,8 @@ struct TileArgs {
     int *overflow_list;    // home cells handed to the overflow kernel
     int *overflow_count;
     int split;             // warps per home cell: the 14 tasks are divided into `split` groups
+    int stage_floats;      // table floats and descriptors staged per CTA (TilePlan)
+    int stage_pots;
 };
 
 // Evaluate one interacting pair, reference orientation I = part_i (home), K = part_j.
@@ -101,7 +103,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
             atomicAdd(&SQ[sb], q - F.half_decay * ssj);
         }
     }
-    const PotDev &pot = pots[pidx];
+    const PotDev pot = pots[pidx];
     if (pot.kind == POT_TABLE) {
         float e, f;
         // radii ride in the staged shift's w component
@@ -138,11 +140,11 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
     }
 }
 
-// Evaluate the queued hits held by the active lanes.  Entries are in enumeration order
-// (i-major), so equal I form contiguous runs: the I side is summed by a segmented warp
-// scan and written by each run's last lane.  Equal K are grouped with match_any and
-// summed into the group's lowest lane.  Every accumulator write is then unique within
-// the batch, so plain shared-memory read-modify-writes suffice.
+// Evaluate the queued hits held by the active lanes.  Entries are in enumeration order, so
+// equal I mostly form contiguous runs: the I side is summed by a segmented warp scan, and
+// run ends that share an I are combined with match_any.  Equal K are grouped with
+// match_any and summed into the group's lowest lane.  Every accumulator write is then
+// unique within the batch, so plain shared-memory read-modify-writes suffice.
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
 __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P, Staged &S, float *SQ,
                                            const PotDev *pots, const float *blob, bool active, uint32_t e, int lane,
@@ -161,20 +163,43 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P
     }
     float4 fI = make_float4(0.f, 0.f, 0.f, 0.f), fK = make_float4(0.f, 0.f, 0.f, 0.f);
     if (active) eval_pair<kDPD, kFlux, kDensity>(T, P, S, SQ, pots, blob, I, K, epot, vir, fI, fK);
-    // I side: segmented inclusive scan over contiguous runs
+    // I side: segmented inclusive scan over runs of contiguous lanes with equal I (a run
+    // starts where I differs from the previous lane's)
     const int key = active ? I : 4096 + lane;
+    const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
+    bool seg = lane == 0 || kprev != key;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const int k2 = __shfl_up_sync(0xffffffffu, key, o);
+        const bool s2 = __shfl_up_sync(0xffffffffu, seg, o);
         const float x = __shfl_up_sync(0xffffffffu, fI.x, o);
         const float y = __shfl_up_sync(0xffffffffu, fI.y, o);
         const float z = __shfl_up_sync(0xffffffffu, fI.z, o);
         const float w = __shfl_up_sync(0xffffffffu, fI.w, o);
-        if (lane >= o && k2 == key) {
+        if (lane >= o && !seg) {
             fI.x += x; fI.y += y; fI.z += z; fI.w += w;
+            seg = s2;
         }
     }
     const int knext = __shfl_down_sync(0xffffffffu, key, 1);
+    // Runs of the same I can recur within a batch (the candidate loop restarts i at each
+    // block of targets): run ends with equal I are combined into the lowest one.
+    const bool run_end = active && (lane == 31 || knext != key);
+    const uint32_t gI = __match_any_sync(0xffffffffu, run_end ? I : 12288 + lane);
+    const uint32_t oI = gI & ~(1u << lane);
+    const int rI = __reduce_max_sync(0xffffffffu, (uint32_t)__popc(oI));
+    const bool leadI = (gI & lanemask_lt()) == 0;
+    uint32_t restI = oI;
+    for (int r = 0; r < rI; r++) {
+        const int src = restI ? __ffs(restI) - 1 : lane;
+        restI &= restI - 1;
+        const float x = __shfl_sync(0xffffffffu, fI.x, src);
+        const float y = __shfl_sync(0xffffffffu, fI.y, src);
+        const float z = __shfl_sync(0xffffffffu, fI.z, src);
+        const float w = __shfl_sync(0xffffffffu, fI.w, src);
+        if (leadI && src != lane) {
+            fI.x += x; fI.y += y; fI.z += z; fI.w += w;
+        }
+    }
     // K side: groups of equal K, summed into the lowest lane of each group
     const int kkey = active ? K : 8192 + lane;
     const uint32_t grp = __match_any_sync(0xffffffffu, kkey);
@@ -193,7 +218,7 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P
             fK.x += x; fK.y += y; fK.z += z; fK.w += w;
         }
     }
-    if (active && (lane == 31 || knext != key)) {
+    if (run_end && leadI) {
         float4 v = S.acc[I];
         v.x += fI.x; v.y += fI.y; v.z += fI.z; v.w += fI.w;
         S.acc[I] = v;
@@ -261,19 +286,21 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Staged *L = reinterpret_cast<Staged *>(smem_raw);
     float *SQall = reinterpret_cast<float *>(smem_raw + sizeof(Staged) * kWarps);
-    float *sblob = SQall + (kFlux ? kWarps * kCapT : 0);
+    PotDev *spot_smem = reinterpret_cast<PotDev *>(SQall + (kFlux ? kWarps * kCapT : 0));
+    float *sblob = reinterpret_cast<float *>(spot_smem + T.stage_pots);
     const PairKernelArgs &a = T.a;
 
-    const int nb = a.blob_floats <= kMaxSmemTable ? a.blob_floats : 0;
-    for (int k = threadIdx.x; k < nb; k += blockDim.x) sblob[k] = a.blob[k];
-    PotDev *spot_smem = reinterpret_cast<PotDev *>(sblob + ((nb + 3) & ~3));
+    // potential descriptors and tables in shared memory when they fit (TilePlan), else
+    // read through L1
     const int npots = a.nsims * a.max_type * a.max_type;
-    const bool stage_pots = npots <= kMaxSmemPots;
-    if (stage_pots)
+    const bool staged = a.blob_floats <= T.stage_floats && npots <= T.stage_pots;
+    if (staged) {
+        for (int k = threadIdx.x; k < a.blob_floats; k += blockDim.x) sblob[k] = a.blob[k];
         for (int k = threadIdx.x; k < npots; k += blockDim.x) spot_smem[k] = a.pots[k];
+    }
     __syncthreads();
-    const float *blob = nb ? sblob : a.blob;
-    const PotDev *spots = stage_pots ? spot_smem : a.pots;
+    const float *blob = staged ? sblob : a.blob;
+    const PotDev *spots = staged ? spot_smem : a.pots;
 
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     Staged &S = L[wid];
@@ -345,22 +372,23 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
             with_self = false;
             int qhead = 0, qtail = 0;
             if (ntgt > 0) {
-                // home particle i (warp-uniform, broadcast) against 32 targets per pass;
-                // self targets (k < nh) only above i
-                for (int i = 0; i < nh; i++) {
-                    const float4 pi4 = S.pos[i];
-                    const float3 xi = make_float3(pi4.x, pi4.y, pi4.z);
-                    const int kfirst = tbeg == 0 ? i + 1 : tbeg;
-                    for (int k0 = kfirst; k0 < end; k0 += 32) {
-                        const int k = k0 + lane;
-                        bool hit = false;
-                        if (k < end) {
-                            const float4 pk = S.pos[k];
-                            const float4 s4 = S.sh4[k];
-                            float3 dx;
-                            const float r2 = pair_r2(xi, make_float3(s4.x, s4.y, s4.z), make_float3(pk.x, pk.y, pk.z), dx);
-                            hit = r2 <= cutoff2;
-                        }
+                // each lane keeps one target k in registers; the home particles i are
+                // broadcast to all lanes.  Self targets (k < nh) pair only with i < k.
+                for (int kb = tbeg; kb < end; kb += 32) {
+                    const int k = kb + lane;
+                    float4 pk = make_float4(0.f, 0.f, 0.f, 0.f), s4 = pk;
+                    if (k < end) {
+                        pk = S.pos[k];
+                        s4 = S.sh4[k];
+                    }
+                    const int ilim = k < end ? (k < nh ? k : nh) : 0;
+                    const int iend = kb + 31 < nh ? kb + 31 : nh;
+                    const float3 xk = make_float3(pk.x, pk.y, pk.z), shk = make_float3(s4.x, s4.y, s4.z);
+                    for (int i = 0; i < iend; i++) {
+                        const float4 pi4 = S.pos[i];
+                        float3 dx;
+                        const float r2 = pair_r2(make_float3(pi4.x, pi4.y, pi4.z), shk, xk, dx);
+                        const bool hit = i < ilim && r2 <= cutoff2;
                         const uint32_t m = __ballot_sync(0xffffffffu, hit);
                         if (hit)
                             S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)k << 16);
@@ -512,9 +540,7 @@ template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
 void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
     const size_t base = sizeof(Staged) * kWarps + (kFlux ? sizeof(float) * kWarps * kCapT : 0);
     const size_t smem_max = base + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxSmemPots;
-    const int nb = T.a.blob_floats <= kMaxSmemTable ? T.a.blob_floats : 0;
-    const int npots = T.a.nsims * T.a.max_type * T.a.max_type;
-    const size_t smem = base + sizeof(float) * ((nb + 3) & ~3) + sizeof(PotDev) * (npots <= kMaxSmemPots ? npots : 0);
+    const size_t smem = base + sizeof(PotDev) * T.stage_pots + sizeof(float) * ((T.stage_floats + 3) & ~3);
     static bool configured = false;
     static size_t occ_smem = 0;
     static int per_sm = 1;
@@ -539,13 +565,24 @@ void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
 
 int pair_tile_capacity() { return kCapT; }
 
-void launch_pair_tile(const PairKernelArgs &a, int *overflow_list, int *overflow_count, int sms, bool signature,
-                      int split, cudaStream_t s) {
+TilePlan plan_pair_tile(int nsims, int max_type, int blob_floats) {
+    TilePlan p;
+    if (blob_floats <= kMaxSmemTable && nsims * max_type * max_type <= kMaxSmemPots) {
+        p.stage_floats = blob_floats;
+        p.stage_pots = nsims * max_type * max_type;
+    }
+    return p;
+}
+
+void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overflow_list, int *overflow_count, int sms,
+                      bool signature, int split, cudaStream_t s) {
     TileArgs T;
     T.a = a;
     T.overflow_list = overflow_list;
     T.overflow_count = overflow_count;
     T.split = (split == 1 || split == 2 || split == 7 || split == 14) ? split : 1;
+    T.stage_floats = plan.stage_floats;
+    T.stage_pots = plan.stage_pots;
     cudaMemsetAsync(overflow_count, 0, sizeof(int), s);
     if (a.n <= 0) return;
     const bool dpd = a.has_dpd, flux = a.nspec > 0 && a.has_flux;
