@@ -72,6 +72,7 @@ struct SimParams {
     float cutoff, cutoff2;
     float dt, dt_flux;
     float maxx[3], maxx2[3], maxv[3], maxv2[3], h2[3];
+    float inv_cutoff;        // 1/cutoff in FP32
     float self_density;      // W(0, cutoff)
     float dpd_delta;         // 1/sqrt(dt) in FP32
     int32_t max_type, nspec;
@@ -204,7 +205,7 @@ __device__ __forceinline__ bool table_eval(const PotDev &p, const float *__restr
     float ee, eff, c1;
     table_row_eval(blob + p.offset + ind * kChunk, r, ee, eff, c1);
     e = ee;
-    f = __fdiv_rn(eff * c1, ro);
+    f = __fdividef(eff * c1, ro);   // within 2 ulp of eff*c1/ro; the interval is already chosen
     return true;
 }
 

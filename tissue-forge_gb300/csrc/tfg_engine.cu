@@ -448,6 +448,7 @@ int add_sim(tfg_engine *eng, const tfg_engine_desc *d, int *out) {
         P.maxv[k] = P.maxx[k] / P.dt;
         P.maxv2[k] = P.maxv[k] * P.maxv[k];
     }
+    P.inv_cutoff = 1.0f / P.cutoff;
     P.self_density = (float)(1.0 / (3.14159265358979323846 * (double)P.cutoff * P.cutoff * P.cutoff));
     P.dpd_delta = 1.f / std::sqrt(P.dt);
     P.max_type = d->max_type;

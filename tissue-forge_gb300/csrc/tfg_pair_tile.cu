@@ -71,7 +71,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
     const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z), sh, make_float3(pk.x, pk.y, pk.z), dx);
     const float r = __fsqrt_rn(r2);
     if (kDensity) {
-        const float w = density_w(r, 1.0f / P.cutoff, P.self_density);
+        const float w = density_w(r, P.inv_cutoff, P.self_density);
         fI.w += w;
         fK.w += w;
     }
@@ -83,7 +83,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
         for (int f = 0; f < fs.count; f++) {
             const FluxDev &F = fs.f[f];
             if (r > F.cutoff) continue;
-            float term = __fsub_rn(1.0f, __fdiv_rn(r, F.cutoff));
+            float term = __fsub_rn(1.0f, __fdividef(r, F.cutoff));
             term = __fmul_rn(term, term);
             const bool a_is_I = (ti == F.type_a);
             const bool b_is_K = (tk == F.type_b);
@@ -122,9 +122,9 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
         if (rr <= pot.b) {
             rr = rr >= pot.a ? rr : pot.a;
             const float4 vi = a.vel[gi], vk = a.vel[gk];
-            const float inv_ro = 1.0f / ro;
+            const float inv_ro = __fdividef(1.0f, ro);
             const float ex = dx.x * inv_ro, ey = dx.y * inv_ro, ez = dx.z * inv_ro;
-            const float omega_c = rr < 0.f ? 1.f : 1.f - rr / pot.b;
+            const float omega_c = rr < 0.f ? 1.f : 1.f - __fdividef(rr, pot.b);
             const float edv = ex * (vi.x - vk.x) + ey * (vi.y - vk.y) + ez * (vi.z - vk.z);
             float xi_r = 1.0f;
             if (!(P.flags & TFG_ENGINE_DPD_REFERENCE_RANDOM))
@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                 const float r = __fsqrt_rn(r2);
                 float4 fi = make_float4(0.f, 0.f, 0.f, 0.f), fj = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (kDensity) {
-                    const float wd = density_w(r, 1.0f / P.cutoff, P.self_density);
+                    const float wd = density_w(r, P.inv_cutoff, P.self_density);
                     fi.w = wd;
                     fj.w = wd;
                 }
@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                     for (int k = 0; k < fs.count; k++) {
                         const FluxDev &F = fs.f[k];
                         if (r > F.cutoff) continue;
-                        float term = __fsub_rn(1.0f, __fdiv_rn(r, F.cutoff));
+                        float term = __fsub_rn(1.0f, __fdividef(r, F.cutoff));
                         term = __fmul_rn(term, term);
                         const int sa = (ti == F.type_a) ? gi : gj, sb = (tj == F.type_b) ? gj : gi;
                         const float ssi = a.sval[F.index_a * a.cap + sa], ssj = a.sval[F.index_b * a.cap + sb];
@@ -513,9 +513,9 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                     if (rr <= pot.b) {
                         rr = rr >= pot.a ? rr : pot.a;
                         const float4 vi = a.vel[gi], vj = a.vel[gj];
-                        const float inv_ro = 1.0f / ro;
+                        const float inv_ro = __fdividef(1.0f, ro);
                         const float ex = dx.x * inv_ro, ey = dx.y * inv_ro, ez = dx.z * inv_ro;
-                        const float omega_c = rr < 0.f ? 1.f : 1.f - rr / pot.b;
+                        const float omega_c = rr < 0.f ? 1.f : 1.f - __fdividef(rr, pot.b);
                         const float edv = ex * (vi.x - vj.x) + ey * (vi.y - vj.y) + ez * (vi.z - vj.z);
                         float xi_r = 1.0f;
                         if (!(P.flags & TFG_ENGINE_DPD_REFERENCE_RANDOM))
