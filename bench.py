@@ -322,6 +322,8 @@ def run_ensemble(args, rank, world, dev, dist):
     cnt0, _ = b.pair_signature()
     pairs0 = int(cnt0.sum()) // 2
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b.set_phase_timing(False)   # the timed steps carry no phase stamps
+    b.step(2)                   # re-capture the step graphs without them
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -337,7 +339,9 @@ def run_ensemble(args, rank, world, dev, dist):
     n_all = int(np.sum(ns_all))
     value = n_all * args.steps / (t_ms * 1e-3)
     step_ms = t_ms / args.steps
-    # phase split and pair-kernel time from a few eager steps after the timed region
+    # phase split and pair-kernel time from a few stamped steps after the timed region
+    b.set_phase_timing(True)
+    b.step(2)
     phase = np.zeros(4)
     for _ in range(5):
         b.step(1)
@@ -483,7 +487,8 @@ def run_single(args, rank, world, dev, dist):
     cnt0, _ = eng.pair_signature()
     pairs0 = int(cnt0.sum()) // 2
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    phase_tot = np.zeros(4)
+    eng.set_phase_timing(False)   # the timed steps carry no phase stamps
+    eng.step(2)                   # re-capture the step graphs without them
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -493,8 +498,17 @@ def run_single(args, rank, world, dev, dist):
             ev[k][0].record(stream)
             eng.step(1, sync=False)
             ev[k][1].record(stream)
-            phase_tot += np.array(eng.phase_ms())
         torch.cuda.synchronize()
+    # phase split from stamped steps after the timed region (L2 flushed before each)
+    eng.set_phase_timing(True)
+    eng.step(2)
+    phase_tot = np.zeros(4)
+    nph = min(args.steps, 10)
+    for k in range(nph):
+        flush.zero_()
+        eng.step(1)
+        phase_tot += np.array(eng.phase_ms())
+    phase_tot *= args.steps / nph
     if dist is not None:
         dist.barrier()
     t_ms = sum(a.elapsed_time(b) for a, b in ev)

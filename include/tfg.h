@@ -230,9 +230,9 @@ TFG_API int tfg_force_only(tfg_engine *eng, int with_bonded);
 TFG_API int tfg_sync(tfg_engine *eng);
 /* *idle = 1 when the engine's stream has no unfinished work, else 0 (never blocks). */
 TFG_API int tfg_query(tfg_engine *eng, int *idle);
-/* Replay steps from CUDA graphs (default on): tfg_step runs its first step eagerly, the
- * middle ones as captured two-step graphs and the last eagerly (with phase events).  A
- * graph is captured again after any change of layout, tables, work split or stream. */
+/* Replay steps from CUDA graphs (default on): after any change of layout, tables, work
+ * split or stream one step runs eagerly, and the following steps replay a captured
+ * single-step graph (one per particle-buffer parity), phase events included. */
 TFG_API int tfg_set_graphs(tfg_engine *eng, int enable);
 /* Autotune the nonbonded pass's work split (warps per home cell: 1, 2, 7 or 14) by timing
  * each choice on the current state; the state is left unchanged.  tfg_step and
@@ -257,9 +257,13 @@ TFG_API int tfg_download(tfg_engine *eng, float *x, float *xrel, int32_t *cell, 
                          float *density, float *species, float *q);
 TFG_API int tfg_get_reductions(tfg_engine *eng, tfg_reductions *out);
 
-/* Per-step timing of the device phases of the last tfg_step call, in milliseconds
- * (CUDA events on the engine stream): [0] bin, [1] pair, [2] bonded, [3] advance. */
+/* Per-step timing of the device phases of the last step, in milliseconds, from GPU
+ * global-timer stamps written between the phases: [0] bin, [1] pair, [2] bonded,
+ * [3] advance (-1 when no step has been timed). */
 TFG_API int tfg_get_phase_ms(tfg_engine *eng, float ms[4]);
+/* Phase stamps on (default) or off: five one-thread kernels per step; turn them off to time
+ * whole steps without them. */
+TFG_API int tfg_set_phase_timing(tfg_engine *eng, int enable);
 
 /* ---- batches: many independent simulations in one device arena ----
  * The reference runs one engine per process (the global `_Engine`, tfEngine.cpp); it has no

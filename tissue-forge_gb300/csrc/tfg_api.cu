@@ -44,12 +44,13 @@ int make_engine(int device, int max_type, int nspec, tfg_engine **out) {
     eng->h_btables.assign(kMaxBondSlots, std::vector<float>());
     int rc;
     if ((rc = dalloc(eng, &eng->err, 1)) || (rc = dalloc(eng, &eng->overflow_count, 1)) ||
-        (rc = dalloc(eng, &eng->bpots, kMaxBondSlots))) {
+        (rc = dalloc(eng, &eng->bpots, kMaxBondSlots)) || (rc = dalloc(eng, &eng->stamps, 5))) {
         destroy(eng);
         return rc;
     }
     cudaMemset(eng->err, 0, sizeof(uint32_t));
     cudaMemset(eng->overflow_count, 0, sizeof(int));
+    cudaMemset(eng->stamps, 0, sizeof(unsigned long long) * 5);
     if (cudaDeviceSynchronize() != cudaSuccess) {
         destroy(eng);
         return TFG_E_CUDA;
@@ -466,13 +467,17 @@ TFG_API int tfg_batch_get_reductions(tfg_engine *eng, int sim, tfg_reductions *o
 
 TFG_API int tfg_get_phase_ms(tfg_engine *eng, float ms[4]) {
     if (!eng || !ms) return TFG_E_INVAL;
+    unsigned long long t[5];
+    CKE(cudaMemcpyAsync(t, eng->stamps, sizeof(t), cudaMemcpyDeviceToHost, eng->stream));
     CKE(cudaStreamSynchronize(eng->stream));
-    for (int k = 0; k < 4; k++) {
-        float t = 0.f;
-        if (cudaEventElapsedTime(&t, eng->ev[k], eng->ev[k + 1]) != cudaSuccess) t = -1.f;
-        ms[k] = t;
-    }
-    cudaGetLastError();
+    for (int k = 0; k < 4; k++) ms[k] = t[k + 1] >= t[k] && t[0] ? (float)((t[k + 1] - t[k]) * 1e-6) : -1.f;
+    return TFG_OK;
+}
+
+TFG_API int tfg_set_phase_timing(tfg_engine *eng, int enable) {
+    if (!eng) return TFG_E_INVAL;
+    if (eng->phase_timing != (enable != 0)) eng->gen++;
+    eng->phase_timing = enable != 0;
     return TFG_OK;
 }
 

@@ -614,14 +614,14 @@ int force_pass(tfg_engine *eng, bool bonded, bool timed) {
                              eng->split, s);
         else launch_pair(a, s);
     }
-    if (timed) cudaEventRecord(eng->ev[2], s);
+    if (timed) launch_stamp(eng->stamps, 2, s);
     if (bonded) {
         launch_bonds(eng->nb, eng->sims_dev, eng->cell_sim, eng->bonds, eng->bond_slot, eng->bpots, eng->bblob,
                      eng->slot_of_id, A.pos, A.aux, A.cell, eng->force, eng->red, s);
         launch_angles(eng->na, eng->sims_dev, eng->cell_sim, eng->angles, eng->bpots, eng->bblob, eng->slot_of_id,
                       A.pos, A.cell, eng->force, eng->red, s);
     }
-    if (timed) cudaEventRecord(eng->ev[3], s);
+    if (timed) launch_stamp(eng->stamps, 3, s);
     return check_launch(eng);
 }
 
@@ -630,16 +630,16 @@ int enqueue_step(tfg_engine *eng, bool advance, bool timed) {
     const int nsims = (int)eng->order.size();
     launch_tick(nsims, eng->sims_dev, s);
     CK(cudaMemsetAsync(eng->red, 0, sizeof(double) * std::max(nsims, 1) * RED_COUNT, s));
-    if (timed) cudaEventRecord(eng->ev[0], s);
+    if (timed) launch_stamp(eng->stamps, 0, s);
     int rc = bin(eng, 1);
     if (rc) return rc;
-    if (timed) cudaEventRecord(eng->ev[1], s);
+    if (timed) launch_stamp(eng->stamps, 1, s);
     rc = force_pass(eng, true, timed);
     if (rc) return rc;
     if (advance)
         launch_advance(eng->n, eng->cap, eng->nspec, eng->sims_dev, eng->cell_sim, eng->A[eng->cur], eng->force,
                        eng->type_mass, eng->type_dyn, eng->species_flags, eng->red, eng->err, s);
-    if (timed) cudaEventRecord(eng->ev[4], s);
+    if (timed) launch_stamp(eng->stamps, 4, s);
     return check_launch(eng);
 }
 
@@ -656,17 +656,18 @@ void drop_graphs(tfg_engine *eng) {
     }
 }
 
-int graph_step_pair(tfg_engine *eng) {
+int graph_step(tfg_engine *eng) {
     const int p = eng->cur;
     if (!eng->graph[p] || eng->graph_gen[p] != eng->gen) {
         if (eng->graph[p]) cudaGraphExecDestroy(eng->graph[p]);
         eng->graph[p] = nullptr;
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(eng->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_step(eng, true, false);
-        if (!rc) rc = enqueue_step(eng, true, false);
+        int rc = enqueue_step(eng, true, eng->phase_timing);
         cudaError_t e = cudaStreamEndCapture(eng->stream, &g);
-        eng->cur = p;  // two buffer swaps: the host view is where it started
+        // the capture swapped the host's buffer index; the replay does the swap for real
+        eng->graph_next[p] = eng->cur;
+        eng->cur = p;
         if (rc || e != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
             cudaGetLastError();
@@ -681,22 +682,25 @@ int graph_step_pair(tfg_engine *eng) {
         eng->graph_gen[p] = eng->gen;
     }
     CK(cudaGraphLaunch(eng->graph[p], eng->stream));
-    for (int k : eng->order) eng->sims[k].time += 2;
+    eng->cur = eng->graph_next[p];
+    for (int k : eng->order) eng->sims[k].time += 1;
     return TFG_OK;
 }
 
 int run_steps(tfg_engine *eng, int nsteps) {
-    // All but the last step in captured pairs (after one eager step has configured every
-    // kernel), the last eagerly with phase events.
-    int k = 0, rc;
-    if (eng->use_graphs && nsteps >= 4) {
-        if ((rc = one_step(eng, true, false))) return rc;
-        k = 1;
-        for (; k + 2 < nsteps; k += 2)
-            if ((rc = graph_step_pair(eng))) return rc;
+    // After any change of the captured launch arguments one step runs eagerly (it also sets
+    // every kernel's launch attributes up); the others replay the captured step of the
+    // current buffer parity.  With phase timing on, every step writes its phase stamps.
+    for (int k = 0; k < nsteps; k++) {
+        int rc;
+        if (eng->use_graphs && eng->eager_gen == eng->gen) {
+            rc = graph_step(eng);
+        } else {
+            rc = one_step(eng, true, eng->phase_timing);
+            eng->eager_gen = eng->gen;
+        }
+        if (rc) return rc;
     }
-    for (; k < nsteps; k++)
-        if ((rc = one_step(eng, true, k == nsteps - 1))) return rc;
     return TFG_OK;
 }
 
@@ -811,7 +815,7 @@ void destroy(tfg_engine *eng) {
     if (eng->stream) cudaStreamSynchronize(eng->stream);
     drop_graphs(eng);
     for (int b = 0; b < 2; b++) free_particles(eng->A[b]);
-    void *bufs[] = {eng->force, eng->count, eng->start, eng->lidx, eng->tmp_id, eng->tmp_src, eng->dest,
+    void *bufs[] = {eng->stamps, eng->force, eng->count, eng->start, eng->lidx, eng->tmp_id, eng->tmp_src, eng->dest,
                     eng->slot_of_id, eng->scan_sums, eng->cell_sim, eng->overflow_list, eng->overflow_count,
                     eng->sims_dev, eng->corig, eng->pots, eng->blob, eng->fluxes, eng->rforce, eng->type_mass,
                     eng->type_dyn, eng->species_flags, eng->bonds, eng->bond_slot, eng->angles, eng->bpots,

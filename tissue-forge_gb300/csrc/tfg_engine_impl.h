@@ -85,25 +85,29 @@ struct tfg_engine {
     uint32_t *err = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
-    cudaEvent_t ev[5] = {};
+    cudaEvent_t ev[5] = {};          // autotuner timing
+    unsigned long long *stamps = nullptr;  // device: global-timer stamps of the phases of a step
+    bool phase_timing = true;
     std::string last_error;
     bool layout_dirty = true, tables_dirty = true;
     bool has_dpd = false, has_flux = false;
     uint32_t flags_all = 0;          // TFG_ENGINE_NO_DENSITY only when every simulation sets it
     int split = 0;                   // tiled pair pass: warps per home cell (0 = not tuned)
     int capacity_hint = 0;
-    // CUDA graphs of two consecutive steps, one per starting buffer parity (a step swaps
-    // the particle buffers, so two steps return to the parity they started from).  `gen`
-    // changes whenever a captured launch argument may have changed (layout, tables, split,
-    // stream); a graph captured under another generation is captured again.
     // tiled-pass staging plan, cached for (generation, split)
     tfg::TilePlan plan;
     uint64_t plan_gen = 0;
     int plan_split = 0;
+    // CUDA graphs of one step, one per starting buffer parity (a step swaps the particle
+    // buffers).  `gen` changes whenever a captured launch argument may have changed
+    // (layout, tables, split, stream); a graph captured under another generation is
+    // captured again, after one eager step of the new generation (`eager_gen`).
     bool use_graphs = true;
     uint64_t gen = 1;
     uint64_t graph_gen[2] = {0, 0};
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_next[2] = {1, 0};      // buffer index after a replay from each parity
+    uint64_t eager_gen = 0;
 };
 
 namespace tfg {
@@ -130,7 +134,7 @@ int bin(tfg_engine *eng, int shuffle);
 int force_pass(tfg_engine *eng, bool bonded, bool timed);
 int one_step(tfg_engine *eng, bool advance, bool timed);
 int enqueue_step(tfg_engine *eng, bool advance, bool timed);  // one_step without the host clock
-int graph_step_pair(tfg_engine *eng);           // two steps replayed from a captured graph
+int graph_step(tfg_engine *eng);                // one step replayed from a captured graph
 int run_steps(tfg_engine *eng, int nsteps);     // nsteps steps, graphs where they apply
 int autotune(tfg_engine *eng);
 PairKernelArgs pair_args(tfg_engine *eng);

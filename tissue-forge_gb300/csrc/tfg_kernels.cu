@@ -51,6 +51,12 @@ __device__ __forceinline__ void keyed_add(double *red, int rb, int slot, float v
     }
 }
 
+__global__ void k_stamp(unsigned long long *t, int k) {
+    unsigned long long v;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(v));
+    t[k] = v;
+}
+
 __global__ void k_tick(int nsims, SimParams *sims) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < nsims) sims[k].time += 1;
@@ -517,6 +523,8 @@ __global__ void k_gather(int n, int slot0, int cap, int nspec, SimParams P, Part
 inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace
+
+void launch_stamp(unsigned long long *t, int k, cudaStream_t s) { k_stamp<<<1, 1, 0, s>>>(t, k); }
 
 void launch_tick(int nsims, SimParams *sims, cudaStream_t s) {
     if (nsims > 0) k_tick<<<nblk(nsims, 128), 128, 0, s>>>(nsims, sims);

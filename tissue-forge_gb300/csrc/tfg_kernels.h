@@ -21,6 +21,9 @@ struct BinArgs {
 };
 
 void launch_tick(int nsims, SimParams *sims, cudaStream_t s);
+// One thread writes the GPU global timer (ns) into t[k]: phase boundaries of a step, valid
+// inside captured graphs (event timing is not).
+void launch_stamp(unsigned long long *t, int k, cudaStream_t s);
 void launch_setpartp(int n, const float *xg, const SimParams &P, float3 lo, float3 hi, float3 org, float3 ih,
                      int slot0, int32_t *cell, float4 *pos, float4 *aux, const int32_t *type, uint32_t *err,
                      cudaStream_t s);

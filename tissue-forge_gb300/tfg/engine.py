@@ -173,6 +173,9 @@ class Engine:
         self._chk(self.L.tfg_get_reductions(self.h, C.byref(r)), "get_reductions")
         return r
 
+    def set_phase_timing(self, enable):
+        self._chk(self.L.tfg_set_phase_timing(self.h, 1 if enable else 0), "set_phase_timing")
+
     def phase_ms(self):
         ms = (C.c_float * 4)()
         self._chk(self.L.tfg_get_phase_ms(self.h, ms), "get_phase_ms")
