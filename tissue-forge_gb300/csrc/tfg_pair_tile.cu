@@ -25,22 +25,32 @@ namespace tfg {
 namespace {
 
 constexpr int kWarps = 8;
-constexpr int kCapT = 160;          // staged particles per warp: home cell + neighbour segments
+constexpr int kCapT = 160;          // staged particles per warp (table variants)
+constexpr int kCapX = 104;          // staged particles per warp (DPD and flux variants)
 constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
 constexpr int kQ = 64;              // candidate ring queue entries per warp (power of two)
 constexpr int kMaxSmemTable = 4096; // floats of potential table staged per CTA
 constexpr int kMaxSmemPots = 64;    // potential descriptors staged per CTA (all simulations)
 
-struct Staged {
-    float4 pos[kCapT];      // cell-relative position; w = type bits
-    float4 acc[kCapT];      // fx, fy, fz, number density (signature: count, hash bits)
-    int32_t gslot[kCapT];   // global slot of the staged particle
-    float4 sh4[kCapT];      // shift of the staged particle's cell as seen from the home cell; w = radius
+// One warp's staging area.  The DPD and flux variants (EXTRA) also stage each particle's
+// velocity, id, species value and flux increment, with fewer particles per warp so that
+// three CTAs still fit an SM.
+template <int CAP, bool EXTRA> struct StagedT {
+    static constexpr int cap = CAP;
+    float4 pos[CAP];        // cell-relative position; w = type bits
+    float4 acc[CAP];        // fx, fy, fz, number density (signature: count, hash bits)
+    int32_t gslot[CAP];     // global slot of the staged particle
+    float4 sh4[CAP];        // shift of the staged particle's cell as seen from the home cell; w = radius
     float sh[27][3];        // shift of each task's partner cell (space_getsid)
     uint32_t q[kQ];         // packed hit (i | k << 16), staged indices
+    float4 vel[EXTRA ? CAP : 1];
+    int32_t id[EXTRA ? CAP : 1];
+    float sv[EXTRA ? CAP : 1];   // species 0 value
+    float sq[EXTRA ? CAP : 1];   // species 0 flux increment
 };
-// Flux increment accumulators (species 0) of one warp's staged particles; allocated only
-// by the flux variants, after the Staged array.
+template <bool kDPD, bool kFlux> struct TileOf {
+    using S = StagedT<(kDPD || kFlux) ? kCapX : kCapT, kDPD || kFlux>;
+};
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
@@ -59,10 +69,10 @@ struct TileArgs {
 
 // Evaluate one interacting pair, reference orientation I = part_i (home), K = part_j.
 // Returns the I-side and K-side increments (force xyz, density) in fI / fK.
-template <bool kDPD, bool kFlux, bool kDensity>
-__device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P, Staged &S, float *SQ,
-                                          const PotDev *pots, const float *blob, int I, int K, float &epot,
-                                          float &vir, float4 &fI, float4 &fK) {
+template <bool kDPD, bool kFlux, bool kDensity, class ST>
+__device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P, ST &S, const PotDev *pots,
+                                          const float *blob, int I, int K, float &epot, float &vir, float4 &fI,
+                                          float4 &fK, float &qI, float &qK) {
     const PairKernelArgs &a = T.a;
     const float4 pi = S.pos[I], pk = S.pos[K];
     const float4 s4 = S.sh4[K];
@@ -77,7 +87,6 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
     }
     const int ti = __float_as_int(pi.w), tk = __float_as_int(pk.w);
     const int pidx = P.pot_base + ti * a.max_type + tk;
-    const int gi = S.gslot[I], gk = S.gslot[K];
     if (kFlux) {
         const FluxSet &fs = a.fluxes[pidx];
         for (int f = 0; f < fs.count; f++) {
@@ -87,8 +96,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
             term = __fmul_rn(term, term);
             const bool a_is_I = (ti == F.type_a);
             const bool b_is_K = (tk == F.type_b);
-            const int sa = a_is_I ? I : K, sb = b_is_K ? K : I;
-            const float ssi = a.sval[a_is_I ? gi : gk], ssj = a.sval[b_is_K ? gk : gi];
+            const float ssi = a_is_I ? S.sv[I] : S.sv[K], ssj = b_is_K ? S.sv[K] : S.sv[I];
             float q = term;
             if (F.kind == TFG_FLUX_FICK) {
                 q = __fmul_rn(q, __fmul_rn(F.coef, __fsub_rn(ssi, ssj)));
@@ -99,8 +107,9 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
                 const float qq = __fmul_rn(__fmul_rn(F.coef, __fsub_rn(F.target, ssj)), ssi);
                 q = __fmul_rn(q, qq > 0.f ? qq : 0.f);
             }
-            atomicAdd(&SQ[sa], -q - F.half_decay * ssi);
-            atomicAdd(&SQ[sb], q - F.half_decay * ssj);
+            const float da = -q - F.half_decay * ssi, db = q - F.half_decay * ssj;
+            if (a_is_I) qI += da; else qK += da;
+            if (b_is_K) qK += db; else qI += db;
         }
     }
     const PotDev pot = pots[pidx];
@@ -115,20 +124,19 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
             vir -= f * r2;
         }
     } else if (kDPD && pot.kind == POT_DPD) {
-        const float4 axi = a.aux[gi], axk = a.aux[gk];
         float rr = r;
         const float ro = r < 1.1920928955078125e-7f ? 1.1920928955078125e-7f : r;
-        if (pot.flags & TFG_POTENTIAL_SHIFTED) rr = __fsub_rn(rr, __fadd_rn(axi.x, axk.x));
+        if (pot.flags & TFG_POTENTIAL_SHIFTED) rr = __fsub_rn(rr, __fadd_rn(S.sh4[I].w, s4.w));
         if (rr <= pot.b) {
             rr = rr >= pot.a ? rr : pot.a;
-            const float4 vi = a.vel[gi], vk = a.vel[gk];
+            const float4 vi = S.vel[I], vk = S.vel[K];
             const float inv_ro = __fdividef(1.0f, ro);
             const float ex = dx.x * inv_ro, ey = dx.y * inv_ro, ez = dx.z * inv_ro;
             const float omega_c = rr < 0.f ? 1.f : 1.f - __fdividef(rr, pot.b);
             const float edv = ex * (vi.x - vk.x) + ey * (vi.y - vk.y) + ez * (vi.z - vk.z);
             float xi_r = 1.0f;
             if (!(P.flags & TFG_ENGINE_DPD_REFERENCE_RANDOM))
-                xi_r = gauss_pair(P.seed, P.time, __float_as_int(axi.w) - P.id_off, __float_as_int(axk.w) - P.id_off);
+                xi_r = gauss_pair(P.seed, P.time, S.id[I] - P.id_off, S.id[K] - P.id_off);
             const float ftot = pot.dpd_alpha * omega_c - pot.dpd_gamma * omega_c * omega_c * edv +
                                pot.dpd_sigma * omega_c * xi_r * P.dpd_delta;
             const float wx = ftot * ex, wy = ftot * ey, wz = ftot * ez;
@@ -145,10 +153,10 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
 // run ends that share an I are combined with match_any.  Equal K are grouped with
 // match_any and summed into the group's lowest lane.  Every accumulator write is then
 // unique within the batch, so plain shared-memory read-modify-writes suffice.
-template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
-__device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P, Staged &S, float *SQ,
-                                           const PotDev *pots, const float *blob, bool active, uint32_t e, int lane,
-                                           float &epot, float &vir) {
+template <bool kDPD, bool kFlux, bool kDensity, bool kSig, class ST>
+__device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P, ST &S, const PotDev *pots,
+                                           const float *blob, bool active, uint32_t e, int lane, float &epot,
+                                           float &vir) {
     const int I = e & 0xffff, K = e >> 16;
     if (kSig) {
         if (active) {
@@ -162,7 +170,8 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P
         return;
     }
     float4 fI = make_float4(0.f, 0.f, 0.f, 0.f), fK = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (active) eval_pair<kDPD, kFlux, kDensity>(T, P, S, SQ, pots, blob, I, K, epot, vir, fI, fK);
+    float qI = 0.f, qK = 0.f;   // species 0 flux increments (flux variants)
+    if (active) eval_pair<kDPD, kFlux, kDensity>(T, P, S, pots, blob, I, K, epot, vir, fI, fK, qI, qK);
     // I side: segmented inclusive scan over runs of contiguous lanes with equal I (a run
     // starts where I differs from the previous lane's)
     const int key = active ? I : 4096 + lane;
@@ -175,8 +184,10 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P
         const float y = __shfl_up_sync(0xffffffffu, fI.y, o);
         const float z = __shfl_up_sync(0xffffffffu, fI.z, o);
         const float w = __shfl_up_sync(0xffffffffu, fI.w, o);
+        const float q = kFlux ? __shfl_up_sync(0xffffffffu, qI, o) : 0.f;
         if (lane >= o && !seg) {
             fI.x += x; fI.y += y; fI.z += z; fI.w += w;
+            if (kFlux) qI += q;
             seg = s2;
         }
     }
@@ -196,8 +207,10 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P
         const float y = __shfl_sync(0xffffffffu, fI.y, src);
         const float z = __shfl_sync(0xffffffffu, fI.z, src);
         const float w = __shfl_sync(0xffffffffu, fI.w, src);
+        const float q = kFlux ? __shfl_sync(0xffffffffu, qI, src) : 0.f;
         if (leadI && src != lane) {
             fI.x += x; fI.y += y; fI.z += z; fI.w += w;
+            if (kFlux) qI += q;
         }
     }
     // K side: groups of equal K, summed into the lowest lane of each group
@@ -214,20 +227,24 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P
         const float y = __shfl_sync(0xffffffffu, fK.y, src);
         const float z = __shfl_sync(0xffffffffu, fK.z, src);
         const float w = __shfl_sync(0xffffffffu, fK.w, src);
+        const float q = kFlux ? __shfl_sync(0xffffffffu, qK, src) : 0.f;
         if (leader && src != lane) {
             fK.x += x; fK.y += y; fK.z += z; fK.w += w;
+            if (kFlux) qK += q;
         }
     }
     if (run_end && leadI) {
         float4 v = S.acc[I];
         v.x += fI.x; v.y += fI.y; v.z += fI.z; v.w += fI.w;
         S.acc[I] = v;
+        if (kFlux) S.sq[I] += qI;
     }
     __syncwarp();
     if (active && leader) {
         float4 v = S.acc[K];
         v.x += fK.x; v.y += fK.y; v.z += fK.z; v.w += fK.w;
         S.acc[K] = v;
+        if (kFlux) S.sq[K] += qK;
     }
 }
 
@@ -246,21 +263,28 @@ __device__ __forceinline__ void flush_red(double *red, int rb, float &epot, floa
     vir = 0.f;
 }
 
-template <bool kFlux, bool kSig>
-__device__ __forceinline__ void stage(const PairKernelArgs &a, Staged &S, float *SQ, int base, int g0, int n,
-                                      int task, int lane) {
+template <bool kDPD, bool kFlux, bool kSig, class ST>
+__device__ __forceinline__ void stage(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane) {
     for (int k = lane; k < n; k += 32) {
-        S.pos[base + k] = a.pos[g0 + k];
+        const int g = g0 + k;
+        const float4 ax = a.aux[g];
+        S.pos[base + k] = a.pos[g];
         S.acc[base + k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        S.gslot[base + k] = g0 + k;
-        S.sh4[base + k] = make_float4(S.sh[task][0], S.sh[task][1], S.sh[task][2], a.aux[g0 + k].x);
-        if (!kSig && kFlux) SQ[base + k] = 0.f;
+        S.gslot[base + k] = g;
+        S.sh4[base + k] = make_float4(S.sh[task][0], S.sh[task][1], S.sh[task][2], ax.x);
+        if (!kSig && kDPD) {
+            S.vel[base + k] = a.vel[g];
+            S.id[base + k] = __float_as_int(ax.w);
+        }
+        if (!kSig && kFlux) {
+            S.sv[base + k] = a.sval[g];
+            S.sq[base + k] = 0.f;
+        }
     }
 }
 
-template <bool kFlux, bool kSig>
-__device__ __forceinline__ void flush(const PairKernelArgs &a, Staged &S, const float *SQ, int b0, int b1,
-                                      int lane) {
+template <bool kFlux, bool kSig, class ST>
+__device__ __forceinline__ void flush(const PairKernelArgs &a, ST &S, int b0, int b1, int lane) {
     for (int k = b0 + lane; k < b1; k += 32) {
         const float4 v = S.acc[k];
         const int g = S.gslot[k];
@@ -275,7 +299,7 @@ __device__ __forceinline__ void flush(const PairKernelArgs &a, Staged &S, const 
         }
         if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(&a.force[g], v);
         if (kFlux) {
-            const float q = SQ[k];
+            const float q = S.sq[k];
             if (q != 0.f) atomicAdd(&a.sq[g], q);
         }
     }
@@ -283,10 +307,11 @@ __device__ __forceinline__ void flush(const PairKernelArgs &a, Staged &S, const 
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
 __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
+    using Staged = typename TileOf<kDPD, kFlux>::S;
+    constexpr int kCap = Staged::cap;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Staged *L = reinterpret_cast<Staged *>(smem_raw);
-    float *SQall = reinterpret_cast<float *>(smem_raw + sizeof(Staged) * kWarps);
-    PotDev *spot_smem = reinterpret_cast<PotDev *>(SQall + (kFlux ? kWarps * kCapT : 0));
+    PotDev *spot_smem = reinterpret_cast<PotDev *>(smem_raw + sizeof(Staged) * kWarps);
     float *sblob = reinterpret_cast<float *>(spot_smem + T.stage_pots);
     const PairKernelArgs &a = T.a;
 
@@ -304,7 +329,6 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
 
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     Staged &S = L[wid];
-    float *SQ = SQall + (kFlux ? wid * kCapT : 0);
     float epot = 0.f, vir = 0.f;
     int cur_rb = -1;
     const int nwarps_total = gridDim.x * kWarps;
@@ -342,7 +366,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
         if (lane == 13) { S.sh[13][0] = 0.f; S.sh[13][1] = 0.f; S.sh[13][2] = 0.f; }
         __syncwarp();
         // capacity: every group of this home cell takes the same decision
-        const bool over = nh > kHomeCap || (lane < 13 && nh + my_n > kCapT);
+        const bool over = nh > kHomeCap || (lane < 13 && nh + my_n > kCap);
         if (__any_sync(0xffffffffu, over)) {
             if (lane == 0 && grp == 0) {
                 const int k = atomicAdd(T.overflow_count, 1);
@@ -350,7 +374,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
             }
             continue;
         }
-        stage<kFlux, kSig>(a, S, SQ, 0, h0, nh, 13, lane);
+        stage<kDPD, kFlux, kSig>(a, S, 0, h0, nh, 13, lane);
         __syncwarp();
 
         int t = t0 < 14 ? 14 : t0;     // next neighbour task to stage
@@ -361,8 +385,8 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
             while (t < t1) {
                 const int g0 = __shfl_sync(0xffffffffu, my_g0, t - 14);
                 const int nn = __shfl_sync(0xffffffffu, my_n, t - 14);
-                if (end + nn > kCapT) break;
-                if (nn > 0) stage<kFlux, kSig>(a, S, SQ, end, g0, nn, t, lane);
+                if (end + nn > kCap) break;
+                if (nn > 0) stage<kDPD, kFlux, kSig>(a, S, end, g0, nn, t, lane);
                 end += nn;
                 t++;
             }
@@ -396,7 +420,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                         __syncwarp();
                         if (qtail - qhead >= 32) {
                             const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
-                            eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, SQ, spots, blob, true, e, lane, epot, vir);
+                            eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, true, e, lane, epot, vir);
                             qhead += 32;
                             __syncwarp();
                         }
@@ -405,14 +429,14 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                 if (qtail > qhead) {
                     const bool act = lane < qtail - qhead;
                     const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
-                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, SQ, spots, blob, act, e, lane, epot, vir);
+                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, lane, epot, vir);
                 }
                 __syncwarp();
             }
-            flush<kFlux, kSig>(a, S, SQ, nh, end, lane);
+            flush<kFlux, kSig>(a, S, nh, end, lane);
             __syncwarp();
         }
-        flush<kFlux, kSig>(a, S, SQ, 0, nh, lane);
+        flush<kFlux, kSig>(a, S, 0, nh, lane);
         __syncwarp();
     }
     if (kSig) return;
@@ -538,7 +562,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
 void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
-    const size_t base = sizeof(Staged) * kWarps + (kFlux ? sizeof(float) * kWarps * kCapT : 0);
+    const size_t base = sizeof(typename TileOf<kDPD, kFlux>::S) * kWarps;
     const size_t smem_max = base + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxSmemPots;
     const size_t smem = base + sizeof(PotDev) * T.stage_pots + sizeof(float) * ((T.stage_floats + 3) & ~3);
     static bool configured = false;
