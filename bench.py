@@ -189,6 +189,19 @@ def fp32_peak(dev):
     return peak.value
 
 
+def profiled_traffic(name, pairs):
+    """DRAM bytes of one pair-kernel launch from the committed ncu summary profiles/<name>
+    (dram__bytes_read.sum + dram__bytes_write.sum of one captured launch), scaled to `pairs`."""
+    try:
+        vals = {}
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if ":" in line and line.split(":")[0] in ("traffic_bytes_per_launch", "pairs_per_launch"):
+                vals[line.split(":")[0]] = float(line.split(":")[1])
+        return vals["traffic_bytes_per_launch"] * pairs / vals["pairs_per_launch"]
+    except Exception:
+        return None
+
+
 def launches_per_step(has_bonds=False, has_angles=False):
     # tick, 7 binning kernels (count, 3 scan passes, place, rank, scatter), the tiled pair
     # kernel and its overflow kernel, bonds, angles, advance
@@ -415,7 +428,11 @@ def run_ensemble(args, rank, world, dev, dist):
             "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
             "peak_source": "measured live (tfg_probe_fp32_tflops, FFMA chains)",
             "flops_per_launch": fl_pair, "pairs_per_step": pairs,
-            "flops_per_pair": FLOPS["table"] + FLOPS["density"], "kernel_ms": phase[1], "traffic": None,
+            "flops_per_pair": FLOPS["table"] + FLOPS["density"], "kernel_ms": phase[1],
+            "traffic": profiled_traffic("k_pair_tile_ensemble256_traffic.md", pairs),
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
+                              "(profiles/k_pair_tile_ensemble256_traffic.md), scaled by pairs",
+            "algorithmic_bytes_per_launch": n_tot * 56,
             "step_hbm": {"achieved_gbs": bytes_alg / (step_ms * 1e-3) / 1e9, "peak_gbs": hbm,
                          "peak_source": hbm_src, "frac": bytes_alg / (step_ms * 1e-3) / 1e9 / hbm,
                          "bytes_per_step": bytes_alg}}
