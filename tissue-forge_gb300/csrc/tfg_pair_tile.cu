@@ -396,40 +396,86 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
             with_self = false;
             int qhead = 0, qtail = 0;
             if (ntgt > 0) {
-                // each lane keeps one target k in registers; the home particles i are
-                // broadcast to all lanes.  Self targets (k < nh) pair only with i < k.
-                for (int kb = tbeg; kb < end; kb += 32) {
-                    const int k = kb + lane;
-                    float4 pk = make_float4(0.f, 0.f, 0.f, 0.f), s4 = pk;
-                    if (k < end) {
-                        pk = S.pos[k];
-                        s4 = S.sh4[k];
-                    }
-                    const int ilim = k < end ? (k < nh ? k : nh) : 0;
-                    const int iend = kb + 31 < nh ? kb + 31 : nh;
-                    const float3 xk = make_float3(pk.x, pk.y, pk.z), shk = make_float3(s4.x, s4.y, s4.z);
-                    for (int i = 0; i < iend; i++) {
-                        const float4 pi4 = S.pos[i];
-                        float3 dx;
-                        const float r2 = pair_r2(make_float3(pi4.x, pi4.y, pi4.z), shk, xk, dx);
-                        const bool hit = i < ilim && r2 <= cutoff2;
-                        const uint32_t m = __ballot_sync(0xffffffffu, hit);
-                        if (hit)
-                            S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)k << 16);
-                        qtail += __popc(m);
+                if constexpr (kDPD || kFlux) {
+                    // The DPD and flux evaluations are long: the candidate walk over (block of 32
+                    // targets, i) pauses whenever 32 hits are queued, so the evaluation has a
+                    // single call site (a second inlined copy costs more in instruction fetch
+                    // than the resumable walk costs in instructions).
+                    int kb = tbeg, i = 0, k = 0, ilim = 0, iend = 0;
+                    float3 xk = make_float3(0.f, 0.f, 0.f), shk = xk;
+                    for (;;) {
+                        while (kb < end && qtail - qhead < 32) {
+                            if (i == 0) {
+                                k = kb + lane;
+                                float4 pk = make_float4(0.f, 0.f, 0.f, 0.f), s4 = pk;
+                                if (k < end) {
+                                    pk = S.pos[k];
+                                    s4 = S.sh4[k];
+                                }
+                                ilim = k < end ? (k < nh ? k : nh) : 0;
+                                iend = kb + 31 < nh ? kb + 31 : nh;
+                                xk = make_float3(pk.x, pk.y, pk.z);
+                                shk = make_float3(s4.x, s4.y, s4.z);
+                            }
+                            const float4 pi4 = S.pos[i];
+                            float3 dx;
+                            const float r2 = pair_r2(make_float3(pi4.x, pi4.y, pi4.z), shk, xk, dx);
+                            const bool hit = i < ilim && r2 <= cutoff2;
+                            const uint32_t m = __ballot_sync(0xffffffffu, hit);
+                            if (hit)
+                                S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)k << 16);
+                            qtail += __popc(m);
+                            if (++i >= iend) {
+                                i = 0;
+                                kb += 32;
+                            }
+                        }
                         __syncwarp();
-                        if (qtail - qhead >= 32) {
-                            const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
-                            eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, true, e, lane, epot, vir);
-                            qhead += 32;
+                        const int avail = qtail - qhead;
+                        if (avail == 0) break;
+                        const int take = avail < 32 ? avail : 32;
+                        const bool act = lane < take;
+                        const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
+                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, lane, epot, vir);
+                        qhead += take;
+                        __syncwarp();
+                    }
+                } else {
+                    // each lane keeps one target k in registers; the home particles i are
+                    // broadcast to all lanes.  Self targets (k < nh) pair only with i < k.
+                    for (int kb = tbeg; kb < end; kb += 32) {
+                        const int k = kb + lane;
+                        float4 pk = make_float4(0.f, 0.f, 0.f, 0.f), s4 = pk;
+                        if (k < end) {
+                            pk = S.pos[k];
+                            s4 = S.sh4[k];
+                        }
+                        const int ilim = k < end ? (k < nh ? k : nh) : 0;
+                        const int iend = kb + 31 < nh ? kb + 31 : nh;
+                        const float3 xk = make_float3(pk.x, pk.y, pk.z), shk = make_float3(s4.x, s4.y, s4.z);
+                        for (int i = 0; i < iend; i++) {
+                            const float4 pi4 = S.pos[i];
+                            float3 dx;
+                            const float r2 = pair_r2(make_float3(pi4.x, pi4.y, pi4.z), shk, xk, dx);
+                            const bool hit = i < ilim && r2 <= cutoff2;
+                            const uint32_t m = __ballot_sync(0xffffffffu, hit);
+                            if (hit)
+                                S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)k << 16);
+                            qtail += __popc(m);
                             __syncwarp();
+                            if (qtail - qhead >= 32) {
+                                const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
+                                eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, true, e, lane, epot, vir);
+                                qhead += 32;
+                                __syncwarp();
+                            }
                         }
                     }
-                }
-                if (qtail > qhead) {
-                    const bool act = lane < qtail - qhead;
-                    const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
-                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, lane, epot, vir);
+                    if (qtail > qhead) {
+                        const bool act = lane < qtail - qhead;
+                        const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
+                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, lane, epot, vir);
+                    }
                 }
                 __syncwarp();
             }
