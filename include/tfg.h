@@ -152,6 +152,8 @@ typedef struct tfg_engine_desc {
     int32_t max_angles;               /* capacity for angles (0 -> sized at load) */
     int32_t device;                   /* CUDA device ordinal */
     uint32_t flags;                   /* TFG_ENGINE_* */
+    int32_t nr_fluxsteps;             /* flux substeps per step, UniverseConfig::nr_fluxsteps
+                                         (tfEngine.cpp:1742, tf_engine_advance.cpp:314-323); 0 -> 1 */
 } tfg_engine_desc;
 
 /* Engine flags.

@@ -177,6 +177,8 @@ template <typename R> struct Engine {
     bool brute = false;          // brute-force pair enumeration instead of sorted windows
     bool ref_dpd_random = false; // reproduce the reference's deterministic DPD "random" term
     bool density = true;
+    bool flux_only = false;      // flux substep pass: fluxes only (runner_*_fluxonly)
+    int nr_fluxsteps = 1;
     R epot_nonbond = 0, epot_bond = 0, epot_angle = 0;
     double kinetic = 0, virial = 0, computed_volume = 0;
     int64_t migrations = 0, straight_angles = 0;
@@ -301,7 +303,9 @@ template <typename R> static int init_space(Engine<R> &e, const tfg_engine_desc 
     e.rf_dur.assign(e.max_type, 1);
     e.species_flags.assign(std::max(1, e.nspec), 0u);
     e.dt = d->dt;
-    e.dt_flux = d->dt;   // nr_fluxsteps == 1: dt_flux = dt / 1 (tfSimulator.cpp:653)
+    // dt_flux = dt / nr_fluxsteps (tfSimulator.cpp:653), an FP32 division
+    e.nr_fluxsteps = d->nr_fluxsteps > 0 ? d->nr_fluxsteps : 1;
+    e.dt_flux = d->dt / (float)e.nr_fluxsteps;
     return TFG_OK;
 }
 
@@ -407,17 +411,17 @@ static inline uint32_t sig_mix(uint32_t id) {
 template <typename R> static void interact(Engine<R> &e, Part<R> &pi, Part<R> &pj, const float *dx,
                                            float r2f, R &epot, double &vir) {
     // per-particle pair signature (each particle's cell is owned by the running task)
-    if (e.want_sig) {
+    if (e.want_sig && !e.flux_only) {
         e.sig_cnt[pi.id]++;
         e.sig_cnt[pj.id]++;
         e.sig_hash[pi.id] += sig_mix((uint32_t)pj.id);
         e.sig_hash[pj.id] += sig_mix((uint32_t)pi.id);
     }
-    if (e.record_pairs) {
+    if (e.record_pairs && !e.flux_only) {
         std::lock_guard<std::mutex> g(e.pair_mtx);
         e.pairs.push_back({std::min(pi.id, pj.id), std::max(pi.id, pj.id)});
     }
-    if (e.density) {
+    if (e.density && !e.flux_only) {
         float nd = Wdens<R>(r2f, e.cutoff);
         pi.f[3] += nd;
         pj.f[3] += nd;
@@ -461,7 +465,7 @@ template <typename R> static void interact(Engine<R> &e, Part<R> &pi, Part<R> &p
             qj = qj + q - half_decay * ssj;
         }
     }
-    if (!pot.set) return;
+    if (!pot.set || e.flux_only) return;
     if (pot.kind == TFG_POTENTIAL_KIND_DPD) {
         // dpd_eval
         const float eps = FLT_EPSILON;
@@ -604,7 +608,7 @@ template <typename R> static void do_self(Engine<R> &e, int cid, R &epot_out) {
     double vir = 0;
     for (int i = 0; i < count; i++) {
         Part<R> &pi = c.parts[i];
-        add_random_force(e, pi);
+        if (!e.flux_only) add_random_force(e, pi);
         for (int j = i + 1; j < count; j++) {
             Part<R> &pj = c.parts[j];
             float dx[3] = {pi.x[0] - pj.x[0], pi.x[1] - pj.x[1], pi.x[2] - pj.x[2]};
@@ -1002,11 +1006,38 @@ template <typename R> static int force_all(Engine<R> &e, bool bonded) {
     return TFG_OK;
 }
 
+// Flux substeps of engine_advance_forward_euler (tf_engine_advance.cpp:314-323): before the
+// step's force evaluation, nr_fluxsteps-1 times a flux-only pass over the same tasks
+// (engine_fluxonly_eval, tfEngine.cpp:1358-1376; runner_dopair_fluxonly / runner_doself_fluxonly,
+// tf_runner_dopair.cpp:334-419, 760-819) followed by Fluxes_integrate over every cell.
+template <typename R> static void flux_substeps(Engine<R> &e) {
+    if (e.nr_fluxsteps <= 1 || e.nspec == 0) return;
+    for (int sub = 0; sub < e.nr_fluxsteps - 1; sub++) {
+        e.flux_only = true;
+        const R ep = e.epot_nonbond;
+        const double vir = e.virial;
+        nonbond(e);
+        e.epot_nonbond = ep;
+        e.virial = vir;
+        e.flux_only = false;
+        for (auto &c : e.cells)
+            for (auto &p : c.parts)
+                for (int s = 0; s < e.nspec; s++) {
+                    float konst = (e.species_flags[s] & 1u) ? 0.f : 1.f;
+                    float &fv = e.svec[(size_t)p.id * e.nspec + s];
+                    R &q = e.sq[(size_t)p.id * e.nspec + s];
+                    fv = std::fmax(0.0f, fv + e.dt_flux * (float)q * konst);
+                    q = 0;
+                }
+    }
+}
+
 template <typename R> static int step(Engine<R> &e) {
     e.time += 1;
     kinetic(e);
     prepare(e);
     shuffle(e);
+    flux_substeps(e);
     force_all(e, true);
     return advance(e);
 }

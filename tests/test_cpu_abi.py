@@ -36,6 +36,7 @@ def test_struct_layouts_match_header():
     # sizes implied by include/tfg.h on LP64
     assert C.sizeof(abi.Potential) == 4 + 4 + 16 + 4 + 4 + 4 + 4 + 8 + 12 + 4  # padded to 8
     assert C.sizeof(abi.Flux) == 36
+    assert C.sizeof(abi.EngineDesc) == 88
     assert C.sizeof(abi.Reductions) == 8 * 7 + 8 * 8 + 16
 
 

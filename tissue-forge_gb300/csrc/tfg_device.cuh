@@ -76,6 +76,7 @@ struct SimParams {
     float self_density;      // W(0, cutoff)
     float dpd_delta;         // 1/sqrt(dt) in FP32
     int32_t max_type, nspec;
+    int32_t nr_fluxsteps;    // flux substeps per step (dt_flux = dt / nr_fluxsteps)
     uint32_t flags;          // TFG_ENGINE_*
     uint64_t seed;
     int64_t time;            // engine time of the step being computed

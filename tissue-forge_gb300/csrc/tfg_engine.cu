@@ -294,6 +294,7 @@ int upload_tables(tfg_engine *eng) {
     for (auto &f : fl) std::memset(&f, 0, sizeof(f));
     eng->has_dpd = false;
     eng->has_flux = false;
+    eng->max_fluxsteps = 1;
     uint32_t nodens = TFG_ENGINE_NO_DENSITY;
     for (size_t q = 0; q < eng->order.size(); q++) {
         SimHost &S = eng->sims[eng->order[q]];
@@ -314,7 +315,10 @@ int upload_tables(tfg_engine *eng) {
                 }
             }
             if (d.kind == POT_DPD) eng->has_dpd = true;
-            if (S.fluxes[k].count > 0) eng->has_flux = true;
+            if (S.fluxes[k].count > 0) {
+                eng->has_flux = true;
+                eng->max_fluxsteps = std::max(eng->max_fluxsteps, S.P.nr_fluxsteps);
+            }
             pots[q * T * T + k] = d;
             fl[q * T * T + k] = S.fluxes[k];
         }
@@ -439,7 +443,6 @@ int add_sim(tfg_engine *eng, const tfg_engine_desc *d, int *out) {
     P.cutoff = d->cutoff;
     P.cutoff2 = d->cutoff * d->cutoff;
     P.dt = d->dt;
-    P.dt_flux = d->dt;
     const float frac = d->particle_max_dist_fraction > 0 ? d->particle_max_dist_fraction : 0.05f;
     for (int k = 0; k < 3; k++) {
         P.h2[k] = 2. * P.h[k];
@@ -453,6 +456,8 @@ int add_sim(tfg_engine *eng, const tfg_engine_desc *d, int *out) {
     P.dpd_delta = 1.f / std::sqrt(P.dt);
     P.max_type = d->max_type;
     P.nspec = d->nr_species;
+    P.nr_fluxsteps = d->nr_fluxsteps > 0 ? d->nr_fluxsteps : 1;
+    P.dt_flux = P.dt / (float)P.nr_fluxsteps;   // tfSimulator.cpp:653
     P.flags = d->flags;
     P.seed = d->seed;
     S.maxc = std::max(P.cdim[0], std::max(P.cdim[1], P.cdim[2]));
@@ -588,6 +593,7 @@ PairKernelArgs pair_args(tfg_engine *eng) {
     a.red = eng->red;
     a.err = eng->err;
     a.has_dpd = eng->has_dpd;
+    a.flux_sub = -1;
     a.has_flux = eng->has_flux;
     return a;
 }
@@ -625,6 +631,23 @@ int force_pass(tfg_engine *eng, bool bonded, bool timed) {
     return check_launch(eng);
 }
 
+// Flux substeps (tf_engine_advance.cpp:314-323): before the step's force pass, each
+// simulation with nr_fluxsteps > 1 runs nr_fluxsteps - 1 flux-only passes over its pair set,
+// each followed by Fluxes_integrate over all its particles with dt_flux.
+int flux_substeps(tfg_engine *eng) {
+    if (!eng->has_flux || eng->nspec == 0 || eng->max_fluxsteps <= 1 || eng->n == 0) return TFG_OK;
+    cudaStream_t s = eng->stream;
+    for (int sub = 0; sub < eng->max_fluxsteps - 1; sub++) {
+        PairKernelArgs a = pair_args(eng);
+        a.flux_sub = sub;
+        launch_pair_fluxonly(a, tile_plan(eng, 1), eng->overflow_list, eng->overflow_count, eng->sms, use_tile(eng), s);
+        ParticleArrays &A = eng->A[eng->cur];
+        launch_flux_integrate(eng->n, eng->cap, eng->nspec, sub, eng->sims_dev, eng->cell_sim, A.cell, A.sval, A.sq,
+                              eng->species_flags, s);
+    }
+    return check_launch(eng);
+}
+
 int enqueue_step(tfg_engine *eng, bool advance, bool timed) {
     cudaStream_t s = eng->stream;
     const int nsims = (int)eng->order.size();
@@ -634,6 +657,7 @@ int enqueue_step(tfg_engine *eng, bool advance, bool timed) {
     int rc = bin(eng, 1);
     if (rc) return rc;
     if (timed) launch_stamp(eng->stamps, 1, s);
+    if ((rc = flux_substeps(eng))) return rc;
     rc = force_pass(eng, true, timed);
     if (rc) return rc;
     if (advance)

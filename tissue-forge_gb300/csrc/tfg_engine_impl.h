@@ -91,6 +91,7 @@ struct tfg_engine {
     std::string last_error;
     bool layout_dirty = true, tables_dirty = true;
     bool has_dpd = false, has_flux = false;
+    int max_fluxsteps = 1;           // largest nr_fluxsteps of a simulation with fluxes
     uint32_t flags_all = 0;          // TFG_ENGINE_NO_DENSITY only when every simulation sets it
     int split = 0;                   // tiled pair pass: warps per home cell (0 = not tuned)
     int capacity_hint = 0;
@@ -133,7 +134,8 @@ int commit(tfg_engine *eng);                    // re-lay the arena out and uplo
 int bin(tfg_engine *eng, int shuffle);
 int force_pass(tfg_engine *eng, bool bonded, bool timed);
 int one_step(tfg_engine *eng, bool advance, bool timed);
-int enqueue_step(tfg_engine *eng, bool advance, bool timed);  // one_step without the host clock
+int enqueue_step(tfg_engine *eng, bool advance, bool timed);
+int flux_substeps(tfg_engine *eng);  // one_step without the host clock
 int graph_step(tfg_engine *eng);                // one step replayed from a captured graph
 int run_steps(tfg_engine *eng, int nsteps);     // nsteps steps, graphs where they apply
 int autotune(tfg_engine *eng);

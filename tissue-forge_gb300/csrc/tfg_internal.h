@@ -67,6 +67,8 @@ struct PairKernelArgs {
     uint32_t *err;
     int32_t *sig_count;         // signature mode: interacting neighbours per particle
     uint32_t *sig_hash;         // signature mode: order-independent hash of neighbour ids
+    int flux_sub;               // >= 0: flux-only substep pass number (simulations with
+                                // nr_fluxsteps - 1 > flux_sub take part); -1: the full pass
     bool has_dpd;               // any type pair uses a DPD potential
     bool has_flux;              // any type pair has fluxes
 };
@@ -89,6 +91,11 @@ TilePlan plan_pair_tile(int nsims, int max_type, int blob_floats);
 void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overflow_list, int *overflow_count, int sms,
                       bool signature, int split, cudaStream_t s);
 int pair_tile_capacity();
+void launch_pair_stencil_fluxonly(const PairKernelArgs &a, cudaStream_t s);
+// Flux-only substep pass (a.flux_sub >= 0): species flux increments of the pair set, no
+// forces, densities or energies (runner_dopair_fluxonly / runner_doself_fluxonly).
+void launch_pair_fluxonly(const PairKernelArgs &a, const TilePlan &plan, int *overflow_list, int *overflow_count,
+                          int sms, bool tile, cudaStream_t s);
 // Same stencil walk and pair decision as launch_pair, writing only the per-particle
 // pair signature (used to prove the pair set bit-exact against the oracle).
 void launch_pair_signature(const PairKernelArgs &a, cudaStream_t s);

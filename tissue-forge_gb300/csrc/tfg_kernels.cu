@@ -488,6 +488,20 @@ __global__ void k_advance(int n, int cap, int nspec, const SimParams *sims, cons
     for (int s = 0; s < nspec; s++) keyed_add(red, rb, RED_SPECIES0 + s, stot[s]);
 }
 
+__global__ void k_flux_integrate(int n, int cap, int nspec, int sub, const SimParams *sims, const int32_t *cell_sim,
+                                 const int32_t *cell, float *sval, float *sq, const uint32_t *species_flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const SimParams &P = sims[cell_sim[cell[i]]];
+    if (sub >= P.nr_fluxsteps - 1) return;
+    for (int s = 0; s < nspec; s++) {
+        const float konst = (species_flags[P.spec_base + s] & 1u) ? 0.f : 1.f;
+        const float q = sq[s * cap + i];
+        sval[s * cap + i] = fmaxf(0.0f, __fadd_rn(sval[s * cap + i], __fmul_rn(__fmul_rn(P.dt_flux, q), konst)));
+        sq[s * cap + i] = 0.f;
+    }
+}
+
 // Per-particle state of slots [slot0, slot0+n) gathered by local id (id - id_off).
 __global__ void k_gather(int n, int slot0, int cap, int nspec, SimParams P, ParticleArrays A, const float4 *force,
                          float *x, float *xrel, int32_t *cellout, float *v, float *f, float *dens, float *species,
@@ -586,6 +600,14 @@ void launch_advance(int n, int cap, int nspec, const SimParams *sims, const int3
         k_advance<<<nblk(n, kThreads), kThreads, 0, s>>>(n, cap, nspec, sims, cell_sim, A.pos, A.vel, A.aux, force,
                                                         A.cell, A.sval, A.sq, type_mass, type_dyn, species_flags, red,
                                                         err);
+}
+
+void launch_flux_integrate(int n, int cap, int nspec, int sub, const SimParams *sims, const int32_t *cell_sim,
+                           const int32_t *cell, float *sval, float *sq, const uint32_t *species_flags,
+                           cudaStream_t s) {
+    if (n > 0 && nspec > 0)
+        k_flux_integrate<<<nblk(n, kThreads), kThreads, 0, s>>>(n, cap, nspec, sub, sims, cell_sim, cell, sval, sq,
+                                                                species_flags);
 }
 
 void launch_gather(int n, int slot0, int cap, int nspec, const SimParams &P, const ParticleArrays &A,

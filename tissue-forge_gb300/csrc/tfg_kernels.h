@@ -39,6 +39,11 @@ void launch_angles(int na, const SimParams *sims, const int32_t *cell_sim, const
 void launch_advance(int n, int cap, int nspec, const SimParams *sims, const int32_t *cell_sim,
                     const ParticleArrays &A, const float4 *force, const float *type_mass, const int32_t *type_dyn,
                     const uint32_t *species_flags, double *red, uint32_t *err, cudaStream_t s);
+// Fluxes_integrate of flux substep `sub` over every particle of the simulations that have
+// that substep (tf_engine_advance.cpp:314-323, tfFlux.cpp:175-202).
+void launch_flux_integrate(int n, int cap, int nspec, int sub, const SimParams *sims, const int32_t *cell_sim,
+                           const int32_t *cell, float *sval, float *sq, const uint32_t *species_flags,
+                           cudaStream_t s);
 void launch_gather(int n, int slot0, int cap, int nspec, const SimParams &P, const ParticleArrays &A,
                    const float4 *force, float *x, float *xrel, int32_t *cell, float *v, float *f, float *dens,
                    float *species, float *q, cudaStream_t s);

@@ -64,7 +64,7 @@ __device__ __forceinline__ void pair_flux(const PairKernelArgs &a, const FluxSet
     }
 }
 
-template <bool kHasFlux, bool kDensity, bool kSig = false>
+template <bool kHasFlux, bool kDensity, bool kSig = false, bool kFluxOnly = false>
 __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a) {
     extern __shared__ float sblob[];
     const int nb = a.blob_floats <= kMaxSmemBlob ? a.blob_floats : 0;
@@ -87,6 +87,8 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
     const int ci = a.cell[i];
     const SimParams &P = a.sims[a.cell_sim[ci]];
     red_base = P.red_base;
+    // flux-only substep pass: only simulations with a substep of this number take part
+    if (!kFluxOnly || a.flux_sub < P.nr_fluxsteps - 1) {
     int li, lj, lk;
     cell_loc(P, ci, li, lj, lk);
 
@@ -152,13 +154,14 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
                 continue;
             }
             const float r = __fsqrt_rn(r2);
-            if (kDensity) acc.dens += density_w(r, inv_cut, P.self_density);
+            if (kDensity && !kFluxOnly) acc.dens += density_w(r, inv_cut, P.self_density);
             const int tj = __float_as_int(pj4.w);
             const int pidx = P.pot_base + ti * a.max_type + tj;
             if (kHasFlux) {
                 const FluxSet &fs = a.fluxes[pidx];
                 if (fs.count) pair_flux<kHasFlux>(a, fs, i_is_pi, ti, tj, i, j, r, acc);
             }
+            if (kFluxOnly) continue;
             const PotDev &pot = a.pots[pidx];
             if (pot.kind == POT_TABLE) {
                 const float rj = a.aux[j].x;
@@ -210,13 +213,14 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
         a.sig_count[idi] = sig_n;
         a.sig_hash[idi] = sig_h;
     } else {
-        a.force[i] = make_float4(acc.fx, acc.fy, acc.fz, acc.dens);
+        if (!kFluxOnly) a.force[i] = make_float4(acc.fx, acc.fy, acc.fz, acc.dens);
         if (kHasFlux) {
             for (int s = 0; s < a.nspec; s++) a.sq[s * a.cap + i] += acc.q[s];
         }
         red_epot = (double)acc.epot;
         red_vir = (double)acc.vir;
     }
+    }  // this simulation takes part
     }  // i < n
     if (kSig) return;
 
@@ -239,6 +243,13 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
 }
 
 }  // namespace
+
+void launch_pair_stencil_fluxonly(const PairKernelArgs &a, cudaStream_t s) {
+    if (a.n <= 0) return;
+    const int blocks = (a.n + kPairThreads - 1) / kPairThreads;
+    const size_t smem = (a.blob_floats <= kMaxSmemBlob ? a.blob_floats : 0) * sizeof(float);
+    k_pair_stencil<true, false, false, true><<<blocks, kPairThreads, smem, s>>>(a);
+}
 
 void launch_pair_signature(const PairKernelArgs &a, cudaStream_t s) {
     if (a.n <= 0) return;

@@ -80,7 +80,8 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
     float3 dx;
     const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z), sh, make_float3(pk.x, pk.y, pk.z), dx);
     const float r = __fsqrt_rn(r2);
-    if (kDensity) {
+    const bool flux_only = kFlux && a.flux_sub >= 0;
+    if (kDensity && !flux_only) {
         const float w = density_w(r, P.inv_cutoff, P.self_density);
         fI.w += w;
         fK.w += w;
@@ -112,6 +113,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
             if (b_is_K) qK += db; else qI += db;
         }
     }
+    if (flux_only) return;
     const PotDev pot = pots[pidx];
     if (pot.kind == POT_TABLE) {
         float e, f;
@@ -340,6 +342,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         if (nh == 0) continue;
         const SimParams &P = a.sims[a.cell_sim[home]];
+        if (kFlux && a.flux_sub >= 0 && a.flux_sub >= P.nr_fluxsteps - 1) continue;
         if (!kSig && P.red_base != cur_rb) {
             flush_red(a.red, cur_rb, epot, vir, lane);
             cur_rb = P.red_base;
@@ -502,6 +505,8 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
         const int home = T.overflow_list[w];
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         const SimParams &P = a.sims[a.cell_sim[home]];
+        const bool flux_only = kFlux && a.flux_sub >= 0;
+        if (flux_only && a.flux_sub >= P.nr_fluxsteps - 1) continue;
         int li, lj, lk;
         cell_loc(P, home, li, lj, lk);
         for (int d = 13; d < 27; d++) {
@@ -537,7 +542,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                 }
                 const float r = __fsqrt_rn(r2);
                 float4 fi = make_float4(0.f, 0.f, 0.f, 0.f), fj = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (kDensity) {
+                if (kDensity && !flux_only) {
                     const float wd = density_w(r, P.inv_cutoff, P.self_density);
                     fi.w = wd;
                     fj.w = wd;
@@ -567,6 +572,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                         atomicAdd(&a.sq[F.index_b * a.cap + sb], q - F.half_decay * ssj);
                     }
                 }
+                if (flux_only) continue;
                 const PotDev &pot = a.pots[pidx];
                 if (pot.kind == POT_TABLE) {
                     float e, f;
@@ -634,6 +640,24 @@ void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
 }  // namespace
 
 int pair_tile_capacity() { return kCapT; }
+
+void launch_pair_fluxonly(const PairKernelArgs &a, const TilePlan &plan, int *overflow_list, int *overflow_count,
+                          int sms, bool tile, cudaStream_t s) {
+    if (!tile) {
+        launch_pair_stencil_fluxonly(a, s);
+        return;
+    }
+    TileArgs T;
+    T.a = a;
+    T.overflow_list = overflow_list;
+    T.overflow_count = overflow_count;
+    T.split = 1;
+    T.stage_floats = plan.stage_floats;
+    T.stage_pots = plan.stage_pots;
+    cudaMemsetAsync(overflow_count, 0, sizeof(int), s);
+    if (a.n <= 0) return;
+    launch_variant<false, true, false, false>(T, s, sms);
+}
 
 TilePlan plan_pair_tile(int nsims, int max_type, int blob_floats) {
     TilePlan p;

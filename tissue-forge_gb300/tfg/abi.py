@@ -72,6 +72,7 @@ class EngineDesc(C.Structure):
         ("nr_species", C.c_int32), ("particle_max_dist_fraction", C.c_float),
         ("seed", C.c_uint64), ("capacity", C.c_int32), ("max_bonds", C.c_int32),
         ("max_angles", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32),
+        ("nr_fluxsteps", C.c_int32),
     ]
 
 
@@ -93,7 +94,7 @@ V_P = C.c_void_p
 
 def engine_desc(origin, dim, cells, cutoff, dt, max_type=1, nr_species=0,
                 particle_max_dist_fraction=0.05, seed=0x5EED, capacity=0,
-                max_bonds=0, max_angles=0, device=0, flags=0):
+                max_bonds=0, max_angles=0, device=0, flags=0, nr_fluxsteps=1):
     d = EngineDesc()
     for k in range(3):
         d.origin[k] = float(origin[k])
@@ -108,6 +109,7 @@ def engine_desc(origin, dim, cells, cutoff, dt, max_type=1, nr_species=0,
     d.capacity = capacity
     d.max_bonds = max_bonds
     d.max_angles = max_angles
+    d.nr_fluxsteps = nr_fluxsteps
     d.device = device
     d.flags = flags
     return d

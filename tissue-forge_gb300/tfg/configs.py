@@ -67,6 +67,7 @@ class Workload:
     relax_steps: int = 0               # overdamped steps before the timed dynamics
     flags: int = 0
     seed: int = 0x5EED
+    nr_fluxsteps: int = 1
 
     @property
     def n(self):
@@ -78,7 +79,8 @@ class Workload:
         return abi.engine_desc(self.origin, self.dim, self.cells, self.cutoff, self.dt,
                                max_type=self.max_type, nr_species=self.nr_species,
                                seed=self.seed, capacity=capacity or self.n,
-                               max_bonds=nb, max_angles=na, device=device, flags=self.flags)
+                               max_bonds=nb, max_angles=na, device=device, flags=self.flags,
+                               nr_fluxsteps=self.nr_fluxsteps)
 
 
 def in_box(x, side):
