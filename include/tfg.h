@@ -166,6 +166,30 @@ typedef struct tfg_engine_desc {
 #define TFG_ENGINE_DPD_REFERENCE_RANDOM (1u << 0)
 #define TFG_ENGINE_NO_DENSITY           (1u << 1)
 
+/* ---- boundary conditions (BoundaryConditions, tfBoundaryConditions.h:39-261) ----
+ * Walls: 0 left (x low), 1 right (x high), 2 front (y low), 3 back (y high), 4 bottom
+ * (z low), 5 top (z high).  Every wall starts PERIODIC.  An axis is periodic when both its
+ * walls are; a PERIODIC wall facing a non-periodic one makes both periodic
+ * (check_periodicy, tfBoundaryConditions.cpp:192-216).  On a non-periodic axis no cell pair
+ * crosses the box edge (space_init task list, tfSpace.cpp:905-1000).  Walls with FREESLIP or
+ * VELOCITY reflect particles that cross them (apply_update_pos_vel,
+ * tf_boundary_eval.h:46-134); NO_SLIP is VELOCITY with zero velocity
+ * (BoundaryCondition::init, tfBoundaryConditions.cpp:151-158).  Potentials set on a wall act
+ * on particles of their type within the potential's range when the wall is active
+ * (FREESLIP, VELOCITY or POTENTIAL; boundary_eval, tf_boundary_eval.h:192-254). */
+#define TFG_BOUNDARY_VELOCITY  (1u << 0)
+#define TFG_BOUNDARY_PERIODIC  (1u << 1)
+#define TFG_BOUNDARY_FREESLIP  (1u << 2)
+#define TFG_BOUNDARY_POTENTIAL (1u << 3)
+#define TFG_BOUNDARY_NO_SLIP   (1u << 4)
+
+typedef struct tfg_boundary {
+    uint32_t kind;         /* TFG_BOUNDARY_* */
+    float velocity[3];     /* wall velocity (VELOCITY) */
+    float restore;         /* fraction of the velocity restored on reflection (default 1) */
+    float radius;          /* wall radius for shifted/scaled wall potentials (default 0) */
+} tfg_boundary;
+
 /* FP64 per-step totals (the reference sums in FPTYPE: tf_engine_advance.cpp:459-470,
  * tfEngine.cpp:1893+). */
 typedef struct tfg_reductions {
@@ -267,6 +291,13 @@ TFG_API int tfg_get_phase_ms(tfg_engine *eng, float ms[4]);
  * whole steps without them. */
 TFG_API int tfg_set_phase_timing(tfg_engine *eng, int enable);
 
+/* Set one wall (0..5) of simulation 0; takes effect at the next step. */
+TFG_API int tfg_set_boundary(tfg_engine *eng, int wall, const tfg_boundary *bc);
+/* Wall potential for particles of `type` (BoundaryCondition::set_potential,
+ * tfBoundaryConditions.cpp:504-513); wall -1 sets all six (BoundaryConditions::set_potential
+ * :559-571); p NULL removes it.  Tables and DPD potentials are accepted. */
+TFG_API int tfg_set_boundary_potential(tfg_engine *eng, int wall, int type, const tfg_potential *p);
+
 /* ---- batches: many independent simulations in one device arena ----
  * The reference runs one engine per process (the global `_Engine`, tfEngine.cpp); it has no
  * counterpart to a batch.  An engine made by tfg_engine_create is a batch holding one
@@ -303,6 +334,8 @@ TFG_API int tfg_batch_get_count(const tfg_engine *eng, int sim, int *n);
 TFG_API int tfg_batch_download(tfg_engine *eng, int sim, float *x, float *xrel, int32_t *cell, float *v,
                                float *f, float *density, float *species, float *q);
 TFG_API int tfg_batch_get_reductions(tfg_engine *eng, int sim, tfg_reductions *out);
+TFG_API int tfg_batch_set_boundary(tfg_engine *eng, int sim, int wall, const tfg_boundary *bc);
+TFG_API int tfg_batch_set_boundary_potential(tfg_engine *eng, int sim, int wall, int type, const tfg_potential *p);
 
 /* Measured FP32 FMA throughput of `device` in TFLOP/s (2 flops per FMA), from a
  * register-only kernel with eight independent FMA chains per thread.  Measurement

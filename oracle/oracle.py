@@ -54,6 +54,8 @@ def lib():
         L.tfo_set_type.argtypes = [E, C.c_int, C.c_int, C.c_float]
         L.tfo_set_potential.argtypes = [E, C.c_int, C.c_int, abi.P_POT]
         L.tfo_add_flux.argtypes = [E, C.c_int, C.c_int, C.POINTER(abi.Flux)]
+        L.tfo_set_boundary.argtypes = [E, C.c_int, C.POINTER(abi.Boundary)]
+        L.tfo_set_boundary_potential.argtypes = [E, C.c_int, C.c_int, abi.P_POT]
         L.tfo_set_species_flags.argtypes = [E, C.c_int, abi.U_P]
         L.tfo_set_random_force.argtypes = [E, C.c_int, C.c_float, C.c_float, C.c_int]
         L.tfo_load_particles.argtypes = [E, C.c_int, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P,
@@ -129,6 +131,13 @@ class OracleEngine:
 
     def add_flux(self, ti, tj, flux):
         _chk(self.L.tfo_add_flux(self.h, ti, tj, C.byref(flux)), "add_flux")
+
+    def set_boundary(self, wall, kind, velocity=(0.0, 0.0, 0.0), restore=1.0, radius=0.0):
+        b = abi.boundary(kind, velocity, restore, radius)
+        _chk(self.L.tfo_set_boundary(self.h, wall, C.byref(b)), "set_boundary")
+
+    def set_boundary_potential(self, wall, t, pot):
+        _chk(self.L.tfo_set_boundary_potential(self.h, wall, t, pot), "set_boundary_potential")
 
     def set_species_flags(self, flags):
         a = np.ascontiguousarray(flags, np.uint32)

@@ -80,7 +80,7 @@ static U4 philox(U4 c, uint32_t k0, uint32_t k1) {
 // (0,1) uniform from 24 high bits.
 static inline float u01(uint32_t u) { return (float)(u >> 8) * 5.9604644775390625e-8f + 2.98023223876953125e-8f; }
 
-enum : uint32_t { STREAM_DPD = 0xD0D0u, STREAM_FORCE = 0xF0F0u, STREAM_ANGLE = 0xA0A0u };
+enum : uint32_t { STREAM_DPD = 0xD0D0u, STREAM_FORCE = 0xF0F0u, STREAM_ANGLE = 0xA0A0u, STREAM_WALL = 0xB0B0u };
 
 // ---------------- reference constants ----------------
 const char kSortID[27] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 0,
@@ -178,6 +178,12 @@ template <typename R> struct Engine {
     bool ref_dpd_random = false; // reproduce the reference's deterministic DPD "random" term
     bool density = true;
     bool flux_only = false;      // flux substep pass: fluxes only (runner_*_fluxonly)
+    // boundary conditions, walls 0..5 = left, right, front, back, bottom, top
+    tfg_boundary walls_set[6];   // as set
+    tfg_boundary walls[6];       // in effect (check_periodicy applied)
+    unsigned periodic = 7;       // bit k: axis k periodic
+    std::vector<Pot<R>> wpots;   // 6 x max_type
+    bool tasks_dirty = false;
     int nr_fluxsteps = 1;
     R epot_nonbond = 0, epot_bond = 0, epot_angle = 0;
     double kinetic = 0, virial = 0, computed_volume = 0;
@@ -233,6 +239,44 @@ template <typename R> static int getsid(const Engine<R> &e, int &ci, int &cj, fl
     return kSortID[sid];
 }
 
+// Task list (space_init, tfSpace.cpp:893-1019): every cell against its neighbours, kept once
+// (id1 < id2) plus self; across the edge of a non-periodic axis there is no neighbour.
+template <typename R> static void build_tasks(Engine<R> &e) {
+    e.tasks.clear();
+    e.sortflags.assign(e.ncells, 0);
+    e.owned.clear();
+    e.colour_classes.clear();
+    for (int i = 0; i < e.cdim[0]; i++)
+        for (int j = 0; j < e.cdim[1]; j++)
+            for (int k = 0; k < e.cdim[2]; k++) {
+                int id1 = cellid(e, i, j, k);
+                for (int a = -1; a <= 1; a++) {
+                    if (!(e.periodic & 1u) && (i + a < 0 || i + a >= e.cdim[0])) continue;
+                    int ii = (i + a + e.cdim[0]) % e.cdim[0];
+                    for (int b = -1; b <= 1; b++) {
+                        if (!(e.periodic & 2u) && (j + b < 0 || j + b >= e.cdim[1])) continue;
+                        int jj = (j + b + e.cdim[1]) % e.cdim[1];
+                        for (int c = -1; c <= 1; c++) {
+                            if (!(e.periodic & 4u) && (k + c < 0 || k + c >= e.cdim[2])) continue;
+                            int kk = (k + c + e.cdim[2]) % e.cdim[2];
+                            int id2 = cellid(e, ii, jj, kk);
+                            int ci = id1, cj = id2;
+                            float sh[3];
+                            int sid = getsid(e, ci, cj, sh);
+                            if (id1 < id2 || (id1 == id2 && a == 0 && b == 0 && c == 0)) {
+                                Task t{id1 == id2 ? 0 : 1, sid, ci, cj};
+                                e.tasks.push_back(t);
+                                if (t.type == 1) {
+                                    e.sortflags[ci] |= 1 << sid;
+                                    e.sortflags[cj] |= 1 << sid;
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+}
+
 template <typename R> static int init_space(Engine<R> &e, const tfg_engine_desc *d) {
     e.d = *d;
     for (int i = 0; i < 3; i++) {
@@ -263,35 +307,14 @@ template <typename R> static int init_space(Engine<R> &e, const tfg_engine_desc 
             }
         }
     }
-    // Task list: every cell against its 26 periodic neighbours, kept once (id1 < id2) plus self.
-    e.tasks.clear();
-    e.sortflags.assign(e.ncells, 0);
-    for (int i = 0; i < e.cdim[0]; i++)
-        for (int j = 0; j < e.cdim[1]; j++)
-            for (int k = 0; k < e.cdim[2]; k++) {
-                int id1 = cellid(e, i, j, k);
-                for (int a = -1; a <= 1; a++) {
-                    int ii = (i + a + e.cdim[0]) % e.cdim[0];
-                    for (int b = -1; b <= 1; b++) {
-                        int jj = (j + b + e.cdim[1]) % e.cdim[1];
-                        for (int c = -1; c <= 1; c++) {
-                            int kk = (k + c + e.cdim[2]) % e.cdim[2];
-                            int id2 = cellid(e, ii, jj, kk);
-                            int ci = id1, cj = id2;
-                            float sh[3];
-                            int sid = getsid(e, ci, cj, sh);
-                            if (id1 < id2 || (id1 == id2 && a == 0 && b == 0 && c == 0)) {
-                                Task t{id1 == id2 ? 0 : 1, sid, ci, cj};
-                                e.tasks.push_back(t);
-                                if (t.type == 1) {
-                                    e.sortflags[ci] |= 1 << sid;
-                                    e.sortflags[cj] |= 1 << sid;
-                                }
-                            }
-                        }
-                    }
-                }
-            }
+    for (int w = 0; w < 6; w++) {
+        std::memset(&e.walls[w], 0, sizeof(tfg_boundary));
+        e.walls[w].kind = TFG_BOUNDARY_PERIODIC;
+        e.walls[w].restore = 1.f;
+        e.walls_set[w] = e.walls[w];
+    }
+    e.periodic = 7;
+    build_tasks(e);
     e.max_type = std::max(1, d->max_type);
     e.nspec = std::max(0, d->nr_species);
     e.pots.assign(e.max_type * e.max_type, Pot<R>());
@@ -302,6 +325,7 @@ template <typename R> static int init_space(Engine<R> &e, const tfg_engine_desc 
     e.rf_std.assign(e.max_type, 0.f);
     e.rf_dur.assign(e.max_type, 1);
     e.species_flags.assign(std::max(1, e.nspec), 0u);
+    e.wpots.assign(6 * e.max_type, Pot<R>());
     e.dt = d->dt;
     // dt_flux = dt / nr_fluxsteps (tfSimulator.cpp:653), an FP32 division
     e.nr_fluxsteps = d->nr_fluxsteps > 0 ? d->nr_fluxsteps : 1;
@@ -601,6 +625,58 @@ template <typename R> static void add_random_force(Engine<R> &e, Part<R> &p) {
     p.fmag += std::sqrt((double)p.pf[0] * p.pf[0] + (double)p.pf[1] * p.pf[1] + (double)p.pf[2] * p.pf[2]);
 }
 
+static inline float wall_gauss(uint64_t seed, int64_t step, int id, int wall) {
+    U4 r = philox({(uint32_t)step, (uint32_t)id, (uint32_t)wall, STREAM_WALL}, (uint32_t)seed, (uint32_t)(seed >> 32));
+    float u1 = u01(r.x), u2 = u01(r.y);
+    return std::sqrt(-2.0f * std::log(u1)) * std::cos(6.283185307179586f * u2);
+}
+
+template <typename R> static bool on_wall(const Engine<R> &e, int w, const int *loc) {
+    const unsigned active = TFG_BOUNDARY_FREESLIP | TFG_BOUNDARY_VELOCITY | TFG_BOUNDARY_POTENTIAL;
+    if (!(e.walls[w].kind & active)) return false;
+    const int ax = w >> 1;
+    return (w & 1) ? loc[ax] + 1 == e.cdim[ax] : loc[ax] == 0;
+}
+
+// boundary_eval (tf_boundary_eval.h:192-254) with boundary_potential_eval_ex (:146-188) and
+// dpd_boundary_eval (tf_dpd_eval.h:78-120): wall potentials of particle p in cell c.
+template <typename R> static void boundary_eval(Engine<R> &e, const Cell<R> &c, Part<R> &p, R &epot) {
+    for (int w = 0; w < 6; w++) {
+        if (!on_wall(e, w, c.loc)) continue;
+        const Pot<R> &pot = e.wpots[w * e.max_type + p.type];
+        if (!pot.set) continue;
+        const int ax = w >> 1;
+        float r = (w & 1) ? e.h[ax] - p.x[ax] : p.x[ax];
+        if (!(r <= pot.b)) continue;
+        const float dxa = (w & 1) ? -r : r;
+        const float r2 = r * r;
+        if (pot.kind == TFG_POTENTIAL_KIND_DPD) {
+            const float eps = FLT_EPSILON;
+            const R delta = (R)(1.f / std::sqrt(e.dt));
+            R rr = std::sqrt((R)r2);
+            R ro = rr < (R)eps ? (R)eps : rr;
+            if (pot.flags & TFG_POTENTIAL_SHIFTED) rr = rr - ((R)p.radius + (R)e.walls[w].radius);
+            if (rr > (R)pot.b) continue;
+            rr = rr >= (R)pot.a ? rr : (R)pot.a;
+            R ea = (R)dxa / ro;
+            R va = (R)p.v[ax] - (R)e.walls[w].velocity[ax];
+            R omega_c = rr < 0 ? (R)1 : (1 - rr / (R)pot.b);
+            R xi = e.ref_dpd_random ? (R)1 : (R)wall_gauss(e.d.seed, e.time, p.id, w);
+            R f = (R)pot.dalpha * omega_c - (R)pot.dgamma * omega_c * omega_c * (ea * va) +
+                  (R)pot.dsigma * omega_c * xi * delta;
+            p.f[ax] += f * ea;
+            p.fmag += std::fabs((double)f);
+        } else {
+            R ee, f;
+            if (pot_eval_ex(pot, p.radius, e.walls[w].radius, r2, (R)r2, ee, f)) {
+                p.f[ax] -= f * (R)dxa;
+                p.fmag += std::fabs((double)f * dxa);
+                epot += ee;
+            }
+        }
+    }
+}
+
 template <typename R> static void do_self(Engine<R> &e, int cid, R &epot_out) {
     Cell<R> &c = e.cells[cid];
     int count = (int)c.parts.size();
@@ -608,7 +684,10 @@ template <typename R> static void do_self(Engine<R> &e, int cid, R &epot_out) {
     double vir = 0;
     for (int i = 0; i < count; i++) {
         Part<R> &pi = c.parts[i];
-        if (!e.flux_only) add_random_force(e, pi);
+        if (!e.flux_only) {
+            add_random_force(e, pi);
+            boundary_eval(e, c, pi, epot);
+        }
         for (int j = i + 1; j < count; j++) {
             Part<R> &pj = c.parts[j];
             float dx[3] = {pi.x[0] - pj.x[0], pi.x[1] - pj.x[1], pi.x[2] - pj.x[2]};
@@ -899,6 +978,30 @@ template <typename R> static void advance_cell(Engine<R> &e, int cid, const floa
         float nd = (float)p.f[3];
         p.v[3] = nd > 0.f ? 1.f / nd : 0.f;
         if (delta[0] || delta[1] || delta[2]) {
+            // apply_update_pos_vel (tf_boundary_eval.h:46-134): reflect at FREESLIP / VELOCITY walls
+            bool enforced = false;
+            for (int w = 0; w < 6; w++) {
+                const tfg_boundary &bw = e.walls[w];
+                if (!(bw.kind & (TFG_BOUNDARY_FREESLIP | TFG_BOUNDARY_VELOCITY)) || !on_wall(e, w, c.loc)) continue;
+                const int ax = w >> 1;
+                const bool high = (w & 1) != 0;
+                if (high ? !(p.x[ax] >= e.h[ax]) : !(p.x[ax] <= 0)) continue;
+                const bool slip = (bw.kind & TFG_BOUNDARY_FREESLIP) != 0;
+                const float rest = slip ? 1.0f : bw.restore;
+                if (high) p.x[ax] = e.h[ax] - std::max<float>((p.x[ax] - e.h[ax]) * rest, FLT_EPSILON);
+                else p.x[ax] = std::max<float>(-p.x[ax] * rest, 0.0f);
+                if (slip) {
+                    p.v[ax] *= -1.0f;
+                } else {
+                    for (int k = 0; k < 3; k++) p.v[k] = bw.velocity[k] - ((p.v[k] - bw.velocity[k]) * rest);
+                }
+                enforced = true;
+            }
+            if (enforced)
+                for (int k = 0; k < 3; k++)
+                    delta[k] = std::isgreaterequal(p.x[k], e.h[k]) - std::isless(p.x[k], 0.0f);
+        }
+        if (delta[0] || delta[1] || delta[2]) {
             for (int k = 0; k < 3; k++) {
                 if (p.x[k] >= h2[k] || p.x[k] <= -e.h[k]) { *err = TFG_E_TOOFAST; break; }
                 float dx = -delta[k] * e.h[k];
@@ -1173,6 +1276,45 @@ TFG_API int tfo_set_potential(tfo_engine *eh, int ti, int tj, const tfg_potentia
         if (!p || ti < 0 || tj < 0 || ti >= e.max_type || tj >= e.max_type) return TFG_E_INVAL;
         copy_pot(e.pots[ti * e.max_type + tj], p);
         copy_pot(e.pots[tj * e.max_type + ti], p);
+        return TFG_OK;
+    };
+    return DISPATCH(h, go);
+}
+
+TFG_API int tfo_set_boundary(tfo_engine *eh, int wall, const tfg_boundary *bc) {
+    Handle *h = reinterpret_cast<Handle *>(eh);
+    auto go = [&](auto &e) {
+        if (!bc || wall < 0 || wall > 5) return TFG_E_INVAL;
+        tfg_boundary b = *bc;
+        if (b.kind & TFG_BOUNDARY_NO_SLIP) {   // BoundaryCondition::init, tfBoundaryConditions.cpp:151-158
+            b.kind = (b.kind & ~TFG_BOUNDARY_NO_SLIP) | TFG_BOUNDARY_VELOCITY;
+            b.velocity[0] = b.velocity[1] = b.velocity[2] = 0.f;
+        }
+        e.walls_set[wall] = b;
+        // check_periodicy (tfBoundaryConditions.cpp:192-216) on the current settings
+        e.periodic = 0;
+        for (int w = 0; w < 6; w++) e.walls[w] = e.walls_set[w];
+        for (int ax = 0; ax < 3; ax++) {
+            tfg_boundary &lo = e.walls[2 * ax], &hi = e.walls[2 * ax + 1];
+            if ((lo.kind & TFG_BOUNDARY_PERIODIC) || (hi.kind & TFG_BOUNDARY_PERIODIC)) {
+                lo.kind = hi.kind = TFG_BOUNDARY_PERIODIC;
+                e.periodic |= 1u << ax;
+            }
+        }
+        build_tasks(e);
+        return TFG_OK;
+    };
+    return DISPATCH(h, go);
+}
+
+TFG_API int tfo_set_boundary_potential(tfo_engine *eh, int wall, int type, const tfg_potential *p) {
+    Handle *h = reinterpret_cast<Handle *>(eh);
+    auto go = [&](auto &e) {
+        if (wall < -1 || wall > 5 || type < 0 || type >= e.max_type) return TFG_E_INVAL;
+        for (int w = (wall < 0 ? 0 : wall); w <= (wall < 0 ? 5 : wall); w++) {
+            if (p) copy_pot(e.wpots[w * e.max_type + type], p);
+            else e.wpots[w * e.max_type + type].set = false;
+        }
         return TFG_OK;
     };
     return DISPATCH(h, go);

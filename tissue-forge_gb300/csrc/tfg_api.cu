@@ -461,6 +461,18 @@ TFG_API int tfg_batch_download(tfg_engine *eng, int sim, float *x, float *xrel, 
 }
 
 TFG_API int tfg_get_reductions(tfg_engine *eng, tfg_reductions *out) { return reductions_sim(eng, 0, out); }
+TFG_API int tfg_set_boundary(tfg_engine *eng, int wall, const tfg_boundary *bc) {
+    return set_boundary_sim(eng, 0, wall, bc);
+}
+TFG_API int tfg_batch_set_boundary(tfg_engine *eng, int sim, int wall, const tfg_boundary *bc) {
+    return set_boundary_sim(eng, sim, wall, bc);
+}
+TFG_API int tfg_set_boundary_potential(tfg_engine *eng, int wall, int type, const tfg_potential *p) {
+    return set_boundary_potential_sim(eng, 0, wall, type, p);
+}
+TFG_API int tfg_batch_set_boundary_potential(tfg_engine *eng, int sim, int wall, int type, const tfg_potential *p) {
+    return set_boundary_potential_sim(eng, sim, wall, type, p);
+}
 TFG_API int tfg_batch_get_reductions(tfg_engine *eng, int sim, tfg_reductions *out) {
     return reductions_sim(eng, sim, out);
 }

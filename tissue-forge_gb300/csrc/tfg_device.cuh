@@ -31,7 +31,7 @@ enum : uint32_t {
 };
 
 // Random streams (Philox4x32-10 counter word 3).
-enum : uint32_t { STREAM_DPD = 0xD0D0u, STREAM_FORCE = 0xF0F0u, STREAM_ANGLE = 0xA0A0u };
+enum : uint32_t { STREAM_DPD = 0xD0D0u, STREAM_FORCE = 0xF0F0u, STREAM_ANGLE = 0xA0A0u, STREAM_WALL = 0xB0B0u };
 
 // One potential as consumed by the kernels (struct Potential, tfPotential.h:213-253).
 // 64 bytes, 16-byte aligned: a descriptor is read with four 128-bit loads.
@@ -81,7 +81,22 @@ struct SimParams {
     uint64_t seed;
     int64_t time;            // engine time of the step being computed
     const float *corig[3];   // cell origin per axis, cdim[k] entries
+    // boundary conditions: walls 0..5 = x low, x high, y low, y high, z low, z high
+    uint32_t periodic;       // bit k: axis k is periodic
+    uint32_t walls_active;   // bit w: wall w is FREESLIP, VELOCITY or POTENTIAL
+    uint32_t walls_reflect;  // bit w: wall w is FREESLIP or VELOCITY
+    uint32_t wall_kind[6];
+    float4 wall_vel[6];      // wall velocity; w = restore
+    float wall_radius[6];
+    int32_t wpot_base;       // (wall 0, type 0) in the wall-potential array; walls x types
 };
+
+// Is wall w of this simulation active and is cell location (a, b, c) on it?
+__host__ __device__ inline bool on_wall(const SimParams &P, int w, int a, int b, int c) {
+    if (!(P.walls_active & (1u << w))) return false;
+    const int l = w < 2 ? a : (w < 4 ? b : c), ax = w >> 1;
+    return (w & 1) ? l + 1 == P.cdim[ax] : l == 0;
+}
 
 // ---------------- Philox4x32-10 (Salmon et al., SC'11) ----------------
 struct U4 { uint32_t x, y, z, w; };
@@ -111,7 +126,21 @@ __device__ __forceinline__ float gauss_pair(uint64_t seed, int64_t step, int ida
     return sqrtf(-2.0f * logf(u1)) * cosf(6.283185307179586f * u2);
 }
 
+// Normal deviate of the DPD wall random term, keyed on (step, particle, wall).
+__device__ __forceinline__ float gauss_wall(uint64_t seed, int64_t step, int id, int wall) {
+    U4 r = philox({(uint32_t)step, (uint32_t)id, (uint32_t)wall, STREAM_WALL}, (uint32_t)seed, (uint32_t)(seed >> 32));
+    float u1 = u01(r.x), u2 = u01(r.y);
+    return sqrtf(-2.0f * logf(u1)) * cosf(6.283185307179586f * u2);
+}
+
 // ---------------- geometry ----------------
+// Does the neighbour at offset o of location l exist along axis ax?  Always on a periodic
+// axis; on a non-periodic one only inside the box (space_init, tfSpace.cpp:913-970).
+__device__ __forceinline__ bool nb_exists(const SimParams &P, int ax, int l, int o) {
+    const int v = l + o;
+    return ((P.periodic >> ax) & 1u) || (v >= 0 && v < P.cdim[ax]);
+}
+
 // Global cell index of the simulation's cell at grid location (i, j, k).
 __device__ __forceinline__ int cell_index(const SimParams &P, int i, int j, int k) {
     return P.cell_off + (i * P.cdim[1] + j) * P.cdim[2] + k;
@@ -208,6 +237,52 @@ __device__ __forceinline__ bool table_eval(const PotDev &p, const float *__restr
     e = ee;
     f = __fdividef(eff * c1, ro);   // within 2 ulp of eff*c1/ro; the interval is already chosen
     return true;
+}
+
+// Wall potentials of one particle in a cell on active walls (boundary_eval,
+// tf_boundary_eval.h:192-254, with boundary_potential_eval_ex :146-188 and dpd_boundary_eval,
+// tf_dpd_eval.h:78-120).  x is cell-relative; the distance to a wall is x (low walls) or
+// h - x (high walls).  Adds the force to f and the energy to epot.
+__device__ __forceinline__ void wall_eval(const SimParams &P, const PotDev *wpots, const float *blob, int type,
+                                          float3 x, float radius, float4 vel, int lid, int la, int lb, int lc,
+                                          float3 &f, float &epot) {
+    for (int w = 0; w < 6; w++) {
+        if (!on_wall(P, w, la, lb, lc)) continue;
+        const PotDev pot = wpots[P.wpot_base + w * P.max_type + type];
+        if (pot.kind == POT_NONE) continue;
+        const int ax = w >> 1;
+        const float xa = ax == 0 ? x.x : (ax == 1 ? x.y : x.z);
+        const float r = (w & 1) ? __fsub_rn(P.h[ax], xa) : xa;
+        if (!(r <= pot.b)) continue;
+        const float dxa = (w & 1) ? -r : r;
+        const float r2 = __fmul_rn(r, r);
+        float fa = 0.f;
+        if (pot.kind == POT_TABLE) {
+            float e, fv;
+            if (table_eval(pot, blob, radius, P.wall_radius[w], r2, e, fv)) {
+                fa = -fv * dxa;   // part->f -= f * dx
+                epot += e;
+            }
+        } else if (pot.kind == POT_DPD) {
+            float rr = __fsqrt_rn(r2);
+            const float ro = rr < 1.1920928955078125e-7f ? 1.1920928955078125e-7f : rr;
+            if (pot.flags & TFG_POTENTIAL_SHIFTED) rr = __fsub_rn(rr, __fadd_rn(radius, P.wall_radius[w]));
+            if (rr > pot.b) continue;
+            rr = rr >= pot.a ? rr : pot.a;
+            const float ea = __fdividef(dxa, ro);
+            const float4 U = P.wall_vel[w];
+            const float va = ax == 0 ? vel.x - U.x : (ax == 1 ? vel.y - U.y : vel.z - U.z);
+            const float omega_c = rr < 0.f ? 1.f : 1.f - __fdividef(rr, pot.b);
+            float xi_r = 1.0f;
+            if (!(P.flags & TFG_ENGINE_DPD_REFERENCE_RANDOM)) xi_r = gauss_wall(P.seed, P.time, lid, w);
+            const float ftot = pot.dpd_alpha * omega_c - pot.dpd_gamma * omega_c * omega_c * (ea * va) +
+                               pot.dpd_sigma * omega_c * xi_r * P.dpd_delta;
+            fa = ftot * ea;   // part->f += f * e
+        }
+        if (ax == 0) f.x += fa;
+        else if (ax == 1) f.y += fa;
+        else f.z += fa;
+    }
 }
 
 }  // namespace tfg

@@ -143,6 +143,8 @@ int relayout(tfg_engine *eng) {
         S.P.type_base = (int)q * T;
         S.P.red_base = (int)q * RED_COUNT;
         S.P.spec_base = (int)q * kMaxSpecies;
+        S.P.wpot_base = (int)q * 6 * T;
+        resolve_boundaries(S);
         S.P.time = S.time;
         N += S.n;
         C += S.P.ncells;
@@ -284,6 +286,9 @@ int upload_tables(tfg_engine *eng) {
     const int T = eng->max_type;
     const size_t nsim = std::max<size_t>(eng->order.size(), 1);
     std::vector<PotDev> pots(nsim * T * T);
+    std::vector<PotDev> wp(nsim * 6 * T);
+    for (auto &p : wp) std::memset(&p, 0, sizeof(p));
+    eng->has_wall_pots = false;
     std::vector<FluxSet> fl(nsim * T * T);
     std::vector<float4> rf(nsim * T, make_float4(0, 0, 1, 0));
     std::vector<float> mass(nsim * T, 1.0f);
@@ -328,6 +333,17 @@ int upload_tables(tfg_engine *eng) {
             dyn[q * T + t] = S.dyn[t];
         }
         for (int k = 0; k < kMaxSpecies; k++) spf[q * kMaxSpecies + k] = S.species_flags[k];
+        for (int k = 0; k < 6 * T; k++) {
+            PotDev d = S.wpots[k];
+            if (d.kind == POT_NONE) continue;
+            eng->has_wall_pots = true;
+            if (d.kind == POT_TABLE) {
+                d.offset = (int)blob.size();
+                blob.insert(blob.end(), S.wtables[k].begin(), S.wtables[k].end());
+            }
+            if (d.kind == POT_DPD) eng->has_dpd = true;
+            wp[q * 6 * T + k] = d;
+        }
     }
     eng->flags_all = nodens;
     if (blob.empty()) blob.push_back(0.f);
@@ -335,8 +351,10 @@ int upload_tables(tfg_engine *eng) {
     if ((rc = ensure(eng, &eng->blob, eng->blob_cap, blob.size())) ||
         (rc = ensure(eng, &eng->pots, eng->pots_cap, pots.size())) ||
         (rc = ensure(eng, &eng->fluxes, eng->fluxes_cap, fl.size())) ||
-        (rc = ensure(eng, &eng->species_flags, eng->spec_cap, spf.size())))
+        (rc = ensure(eng, &eng->species_flags, eng->spec_cap, spf.size())) ||
+        (rc = ensure(eng, &eng->wpots, eng->wpots_cap, wp.size())))
         return rc;
+    CK(cudaMemcpyAsync(eng->wpots, wp.data(), sizeof(PotDev) * wp.size(), cudaMemcpyHostToDevice, s));
     if (rf.size() > eng->types_cap) {
         if ((rc = dalloc(eng, &eng->rforce, rf.size())) || (rc = dalloc(eng, &eng->type_mass, rf.size())) ||
             (rc = dalloc(eng, &eng->type_dyn, rf.size())))
@@ -416,6 +434,75 @@ PotDev to_dev(const tfg_potential *p) {
     return d;
 }
 
+// Periodicity and wall flags of a simulation from its six walls as set (BoundaryConditions,
+// tfBoundaryConditions.cpp:192-216 and space_init's cell flags, tfSpace.cpp:780-835): a
+// periodic wall facing a non-periodic one makes both periodic.  Walls are set one at a
+// time, so the rule is applied to the current settings, which stay as set.
+void resolve_boundaries(SimHost &S) {
+    SimParams &P = S.P;
+    P.periodic = 0;
+    P.walls_active = 0;
+    P.walls_reflect = 0;
+    uint32_t kind[6];
+    for (int w = 0; w < 6; w++) kind[w] = S.walls[w].kind;
+    for (int ax = 0; ax < 3; ax++) {
+        if ((kind[2 * ax] | kind[2 * ax + 1]) & TFG_BOUNDARY_PERIODIC) {
+            kind[2 * ax] = kind[2 * ax + 1] = TFG_BOUNDARY_PERIODIC;
+            P.periodic |= 1u << ax;
+        }
+    }
+    const uint32_t active = TFG_BOUNDARY_FREESLIP | TFG_BOUNDARY_VELOCITY | TFG_BOUNDARY_POTENTIAL;
+    for (int w = 0; w < 6; w++) {
+        const tfg_boundary &b = S.walls[w];
+        P.wall_kind[w] = kind[w];
+        P.wall_vel[w] = make_float4(b.velocity[0], b.velocity[1], b.velocity[2], b.restore);
+        P.wall_radius[w] = b.radius;
+        if (kind[w] & active) P.walls_active |= 1u << w;
+        if (kind[w] & (TFG_BOUNDARY_FREESLIP | TFG_BOUNDARY_VELOCITY)) P.walls_reflect |= 1u << w;
+    }
+}
+
+int set_boundary_sim(tfg_engine *eng, int sim, int wall, const tfg_boundary *bc) {
+    int rc = sim_check(eng, sim);
+    if (rc) return rc;
+    if (wall < 0 || wall > 5 || !bc) return fail(eng, TFG_E_INVAL, "wall must be 0..5");
+    tfg_boundary b = *bc;
+    if (b.kind & TFG_BOUNDARY_NO_SLIP) {
+        b.kind = (b.kind & ~TFG_BOUNDARY_NO_SLIP) | TFG_BOUNDARY_VELOCITY;
+        b.velocity[0] = b.velocity[1] = b.velocity[2] = 0.f;
+    }
+    SimHost &S = eng->sims[sim];
+    S.walls[wall] = b;
+    resolve_boundaries(S);
+    eng->layout_dirty = true;   // parameters are uploaded with the layout
+    return TFG_OK;
+}
+
+int set_boundary_potential_sim(tfg_engine *eng, int sim, int wall, int type, const tfg_potential *p) {
+    int rc = sim_check(eng, sim);
+    if (rc) return rc;
+    const int T = eng->max_type;
+    if (wall < -1 || wall > 5 || type < 0 || type >= T) return fail(eng, TFG_E_INVAL, "bad wall or type");
+    SimHost &S = eng->sims[sim];
+    for (int w = (wall < 0 ? 0 : wall); w <= (wall < 0 ? 5 : wall); w++) {
+        const int k = w * T + type;
+        if (!p) {
+            std::memset(&S.wpots[k], 0, sizeof(PotDev));
+            S.wtables[k].clear();
+            continue;
+        }
+        if (p->kind == TFG_POTENTIAL_KIND_POTENTIAL) {
+            if (!p->c || p->n < 1 || p->n > TFG_POTENTIAL_IVALSMAX) return fail(eng, TFG_E_INVAL, "bad table");
+            S.wtables[k].assign(p->c, p->c + (size_t)(p->n + 1) * kChunk);
+        } else if (p->kind != TFG_POTENTIAL_KIND_DPD) {
+            return fail(eng, TFG_E_INVAL, "unsupported potential kind");
+        }
+        S.wpots[k] = to_dev(p);
+    }
+    eng->tables_dirty = true;
+    return TFG_OK;
+}
+
 // A new simulation: space geometry (space_init, tfSpace.cpp:737-777) and integrator
 // limits (tf_engine_advance.cpp:337-350).
 int add_sim(tfg_engine *eng, const tfg_engine_desc *d, int *out) {
@@ -475,6 +562,15 @@ int add_sim(tfg_engine *eng, const tfg_engine_desc *d, int *out) {
     S.mass.assign(T, 1.0f);
     S.dyn.assign(T, TFG_NEWTONIAN);
     S.species_flags.assign(kMaxSpecies, 0u);
+    for (int w = 0; w < 6; w++) {
+        std::memset(&S.walls[w], 0, sizeof(tfg_boundary));
+        S.walls[w].kind = TFG_BOUNDARY_PERIODIC;
+        S.walls[w].restore = 1.f;
+    }
+    S.wpots.resize(6 * T);
+    for (auto &p : S.wpots) std::memset(&p, 0, sizeof(p));
+    S.wtables.assign(6 * T, std::vector<float>());
+    resolve_boundaries(S);
     eng->sims.push_back(std::move(S));
     if (out) *out = (int)eng->sims.size() - 1;
     return TFG_OK;
@@ -588,6 +684,8 @@ PairKernelArgs pair_args(tfg_engine *eng) {
     a.blob = eng->blob;
     a.blob_floats = eng->blob_floats;
     a.fluxes = eng->fluxes;
+    a.wpots = eng->wpots;
+    a.has_wall_pots = eng->has_wall_pots;
     a.rforce = eng->rforce;
     a.pforce_out = A.pforce;
     a.red = eng->red;
@@ -839,7 +937,7 @@ void destroy(tfg_engine *eng) {
     if (eng->stream) cudaStreamSynchronize(eng->stream);
     drop_graphs(eng);
     for (int b = 0; b < 2; b++) free_particles(eng->A[b]);
-    void *bufs[] = {eng->stamps, eng->force, eng->count, eng->start, eng->lidx, eng->tmp_id, eng->tmp_src, eng->dest,
+    void *bufs[] = {eng->wpots, eng->stamps, eng->force, eng->count, eng->start, eng->lidx, eng->tmp_id, eng->tmp_src, eng->dest,
                     eng->slot_of_id, eng->scan_sums, eng->cell_sim, eng->overflow_list, eng->overflow_count,
                     eng->sims_dev, eng->corig, eng->pots, eng->blob, eng->fluxes, eng->rforce, eng->type_mass,
                     eng->type_dyn, eng->species_flags, eng->bonds, eng->bond_slot, eng->angles, eng->bpots,

@@ -42,6 +42,9 @@ struct SimHost {
     std::vector<int32_t> bond_slot;
     std::vector<int4> angles;        // local ids, w = slot
     int64_t time = 0;
+    tfg_boundary walls[6];           // as set (NO_SLIP already turned into VELOCITY)
+    std::vector<tfg::PotDev> wpots;  // 6 x max_type wall potentials
+    std::vector<std::vector<float>> wtables;
 };
 
 struct tfg_engine {
@@ -75,6 +78,9 @@ struct tfg_engine {
     int32_t *bond_slot = nullptr;
     int4 *angles = nullptr;
     int nb = 0, na = 0, bcap = 0, acap = 0;
+    tfg::PotDev *wpots = nullptr;     // nsims x 6 x max_type wall potentials
+    size_t wpots_cap = 0;
+    bool has_wall_pots = false;
     tfg::PotDev *bpots = nullptr;
     float *bblob = nullptr;
     size_t bblob_cap = 0;
@@ -149,6 +155,9 @@ int load_sim(tfg_engine *eng, int sim, int n, const float *xg, const int32_t *ce
 int download_sim(tfg_engine *eng, int sim, float *x, float *xrel, int32_t *cell, float *v, float *f, float *dens,
                  float *species, float *q);
 int reductions_sim(tfg_engine *eng, int sim, tfg_reductions *out);
+int set_boundary_sim(tfg_engine *eng, int sim, int wall, const tfg_boundary *bc);
+int set_boundary_potential_sim(tfg_engine *eng, int sim, int wall, int type, const tfg_potential *p);
+void resolve_boundaries(SimHost &S);   // periodicity and wall flags into S.P
 void destroy(tfg_engine *eng);
 
 }  // namespace tfg

@@ -60,6 +60,8 @@ struct PairKernelArgs {
     const PotDev *pots;         // nsims * max_type^2
     const float *blob;
     int blob_floats;
+    const PotDev *wpots;        // nsims * 6 * max_type wall potentials
+    bool has_wall_pots;         // any simulation has a wall potential
     const FluxSet *fluxes;      // nsims * max_type^2
     const float4 *rforce;       // nsims * max_type: mean, std, duration, enabled
     float4 *pforce_out;         // persistent force updated in place (same as pforce)

@@ -452,6 +452,34 @@ __global__ void k_advance(int n, int cap, int nspec, const SimParams *sims, cons
             const float nd = f.w;
             const float inv_nd = nd > 0.f ? __fdiv_rn(1.f, nd) : 0.f;
             vol = inv_nd;
+            if ((delta[0] | delta[1] | delta[2]) && P.walls_reflect) {
+                // reflection at FREESLIP / VELOCITY walls (apply_update_pos_vel,
+                // tf_boundary_eval.h:46-134), walls in the reference's order
+                int la, lb, lc;
+                cell_loc(P, c0, la, lb, lc);
+                bool enforced = false;
+                for (int w = 0; w < 6; w++) {
+                    if (!(P.walls_reflect & (1u << w)) || !on_wall(P, w, la, lb, lc)) continue;
+                    const int ax = w >> 1;
+                    const bool high = (w & 1) != 0;
+                    if (high ? !(x[ax] >= P.h[ax]) : !(x[ax] <= 0.f)) continue;
+                    const bool slip = (P.wall_kind[w] & TFG_BOUNDARY_FREESLIP) != 0;
+                    const float rest = slip ? 1.0f : P.wall_vel[w].w;
+                    if (high)
+                        x[ax] = __fsub_rn(P.h[ax], fmaxf(__fmul_rn(__fsub_rn(x[ax], P.h[ax]), rest), 1.1920928955078125e-7f));
+                    else
+                        x[ax] = fmaxf(__fmul_rn(-x[ax], rest), 0.0f);
+                    if (slip) {
+                        vv[ax] = -vv[ax];
+                    } else {
+                        const float U[3] = {P.wall_vel[w].x, P.wall_vel[w].y, P.wall_vel[w].z};
+                        for (int k = 0; k < 3; k++) vv[k] = __fsub_rn(U[k], __fmul_rn(__fsub_rn(vv[k], U[k]), rest));
+                    }
+                    enforced = true;
+                }
+                if (enforced)
+                    for (int k = 0; k < 3; k++) delta[k] = (x[k] >= P.h[k]) - (x[k] < 0.0f);
+            }
             if (delta[0] | delta[1] | delta[2]) {
                 for (int k = 0; k < 3; k++) {
                     if (x[k] >= P.h2[k] || x[k] <= -P.h[k]) { atomicOr(err, ERR_TOOFAST); break; }

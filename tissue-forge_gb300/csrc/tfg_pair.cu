@@ -107,11 +107,21 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
 
     int sig_n = 0;
     uint32_t sig_h = 0;
+    if (!kSig && !kFluxOnly && a.has_wall_pots && P.walls_active) {
+        float3 fw = make_float3(0.f, 0.f, 0.f);
+        float ew = 0.f;
+        wall_eval(P, a.wpots, blob, ti, xi, ri, vi4, idi - P.id_off, li, lj, lk, fw, ew);
+        acc.fx += fw.x;
+        acc.fy += fw.y;
+        acc.fz += fw.z;
+        acc.epot += ew;
+    }
     for (int d = 0; d < 27; d++) {
         const int ox = d / 9 - 1, oy = (d / 3) % 3 - 1, oz = d % 3 - 1;
         const int mi = li + ox < 0 ? li + ox + P.cdim[0] : (li + ox >= P.cdim[0] ? li + ox - P.cdim[0] : li + ox);
         const int mj = lj + oy < 0 ? lj + oy + P.cdim[1] : (lj + oy >= P.cdim[1] ? lj + oy - P.cdim[1] : lj + oy);
         const int mk = lk + oz < 0 ? lk + oz + P.cdim[2] : (lk + oz >= P.cdim[2] ? lk + oz - P.cdim[2] : lk + oz);
+        if (!(nb_exists(P, 0, li, ox) && nb_exists(P, 1, lj, oy) && nb_exists(P, 2, lk, oz))) continue;
         const int cj = cell_index(P, mi, mj, mk);
         const int j0 = a.start[cj], j1 = a.start[cj + 1];
         const bool self = (d == 13);

@@ -362,6 +362,8 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
             const int c = cell_index(P, mi, mj, mk);
             my_g0 = a.start[c];
             my_n = a.start[c + 1] - my_g0;
+            // no cell pair across the edge of a non-periodic axis
+            if (!(nb_exists(P, 0, li, ox) && nb_exists(P, 1, lj, oy) && nb_exists(P, 2, lk, oz))) my_n = 0;
             S.sh[d][0] = cell_shift(P, 0, li, mi);
             S.sh[d][1] = cell_shift(P, 1, lj, mj);
             S.sh[d][2] = cell_shift(P, 2, lk, mk);
@@ -379,6 +381,23 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
         }
         stage<kDPD, kFlux, kSig>(a, S, 0, h0, nh, 13, lane);
         __syncwarp();
+        // wall potentials of the home particles, once per home cell (runner_doself's
+        // boundary_eval, tf_runner_dopair.cpp:594-596)
+        if (!kSig && t0 == 13 && a.has_wall_pots && P.walls_active && !(kFlux && a.flux_sub >= 0)) {
+            for (int k = lane; k < nh; k += 32) {
+                const float4 p4 = S.pos[k];
+                const int g = S.gslot[k];
+                float3 fw = make_float3(0.f, 0.f, 0.f);
+                float ew = 0.f;
+                wall_eval(P, a.wpots, blob, __float_as_int(p4.w), make_float3(p4.x, p4.y, p4.z), S.sh4[k].w,
+                          a.vel[g], __float_as_int(a.aux[g].w) - P.id_off, li, lj, lk, fw, ew);
+                S.acc[k].x += fw.x;
+                S.acc[k].y += fw.y;
+                S.acc[k].z += fw.z;
+                epot += ew;
+            }
+            __syncwarp();
+        }
 
         int t = t0 < 14 ? 14 : t0;     // next neighbour task to stage
         bool with_self = (t0 == 13);
@@ -509,12 +528,25 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
         if (flux_only && a.flux_sub >= P.nr_fluxsteps - 1) continue;
         int li, lj, lk;
         cell_loc(P, home, li, lj, lk);
+        if (!kSig && !flux_only && a.has_wall_pots && P.walls_active) {
+            for (int i = lane; i < nh; i += 32) {
+                const int g = h0 + i;
+                const float4 p4 = a.pos[g], ax4 = a.aux[g];
+                float3 fw = make_float3(0.f, 0.f, 0.f);
+                float ew = 0.f;
+                wall_eval(P, a.wpots, a.blob, __float_as_int(p4.w), make_float3(p4.x, p4.y, p4.z), ax4.x, a.vel[g],
+                          __float_as_int(ax4.w) - P.id_off, li, lj, lk, fw, ew);
+                if (fw.x != 0.f || fw.y != 0.f || fw.z != 0.f) atomicAdd(&a.force[g], make_float4(fw.x, fw.y, fw.z, 0.f));
+                epot += ew;
+            }
+        }
         for (int d = 13; d < 27; d++) {
             const int ox = d / 9 - 1, oy = (d / 3) % 3 - 1, oz = d % 3 - 1;
             const bool self = d == 13;
             const int mi = (li + ox + P.cdim[0]) % P.cdim[0];
             const int mj = (lj + oy + P.cdim[1]) % P.cdim[1];
             const int mk = (lk + oz + P.cdim[2]) % P.cdim[2];
+            if (!(nb_exists(P, 0, li, ox) && nb_exists(P, 1, lj, oy) && nb_exists(P, 2, lk, oz))) continue;
             const int c = cell_index(P, mi, mj, mk);
             const int g0 = a.start[c], nn = a.start[c + 1] - g0;
             float3 sh = make_float3(0.f, 0.f, 0.f);

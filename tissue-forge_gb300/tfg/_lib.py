@@ -61,6 +61,10 @@ def lib():
     L.tfg_probe_fp32_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.tfg_bin_noalloc.argtypes = [C.POINTER(abi.EngineDesc), C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_void_p, C.c_void_p, C.c_void_p]
+    L.tfg_set_boundary.argtypes = [E, C.c_int, C.POINTER(abi.Boundary)]
+    L.tfg_set_boundary_potential.argtypes = [E, C.c_int, C.c_int, abi.P_POT]
+    L.tfg_batch_set_boundary.argtypes = [E, C.c_int, C.c_int, C.POINTER(abi.Boundary)]
+    L.tfg_batch_set_boundary_potential.argtypes = [E, C.c_int, C.c_int, C.c_int, abi.P_POT]
     L.tfg_batch_create.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(E)]
     L.tfg_batch_add_sim.argtypes = [E, C.POINTER(abi.EngineDesc), C.POINTER(C.c_int)]
     L.tfg_batch_remove_sim.argtypes = [E, C.c_int]

@@ -36,6 +36,13 @@ FLUX_FICK = 0
 FLUX_SECRETE = 1
 FLUX_UPTAKE = 2
 
+# boundary kinds (tfBoundaryConditions.h:39-45); walls 0..5 = left, right, front, back, bottom, top
+BOUNDARY_VELOCITY = 1 << 0
+BOUNDARY_PERIODIC = 1 << 1
+BOUNDARY_FREESLIP = 1 << 2
+BOUNDARY_POTENTIAL = 1 << 3
+BOUNDARY_NO_SLIP = 1 << 4
+
 NEWTONIAN = 0
 OVERDAMPED = 1
 
@@ -74,6 +81,20 @@ class EngineDesc(C.Structure):
         ("max_angles", C.c_int32), ("device", C.c_int32), ("flags", C.c_uint32),
         ("nr_fluxsteps", C.c_int32),
     ]
+
+
+class Boundary(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("velocity", C.c_float * 3), ("restore", C.c_float), ("radius", C.c_float)]
+
+
+def boundary(kind, velocity=(0.0, 0.0, 0.0), restore=1.0, radius=0.0):
+    b = Boundary()
+    b.kind = kind
+    for k in range(3):
+        b.velocity[k] = float(velocity[k])
+    b.restore = restore
+    b.radius = radius
+    return b
 
 
 class Reductions(C.Structure):

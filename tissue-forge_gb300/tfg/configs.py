@@ -68,6 +68,8 @@ class Workload:
     flags: int = 0
     seed: int = 0x5EED
     nr_fluxsteps: int = 1
+    boundaries: list = field(default_factory=list)  # (wall, kind, velocity, restore, radius)
+    wall_pots: list = field(default_factory=list)   # (wall or -1, type, PotSpec)
 
     @property
     def n(self):

@@ -84,6 +84,14 @@ class Engine:
         ptr = pot.ptr if isinstance(pot, Potential) else pot
         self._chk(self.L.tfg_set_bonded_potential(self.h, slot, ptr), "set_bonded_potential")
 
+    def set_boundary(self, wall, kind, velocity=(0.0, 0.0, 0.0), restore=1.0, radius=0.0):
+        b = abi.boundary(kind, velocity, restore, radius)
+        self._chk(self.L.tfg_set_boundary(self.h, wall, C.byref(b)), "set_boundary")
+
+    def set_boundary_potential(self, wall, t, pot):
+        ptr = pot.ptr if isinstance(pot, Potential) else pot
+        self._chk(self.L.tfg_set_boundary_potential(self.h, wall, t, ptr), "set_boundary_potential")
+
     def load(self, x, v=None, type=None, radius=None, imass=None, flags=None, species=None, force_i=None):
         x = np.ascontiguousarray(x, np.float32)
         self.n = x.shape[0]
@@ -265,6 +273,15 @@ class Sim:
     def set_bonded_potential(self, slot, pot):
         self.b.set_bonded_potential(slot, pot)
 
+    def set_boundary(self, wall, kind, velocity=(0.0, 0.0, 0.0), restore=1.0, radius=0.0):
+        b = abi.boundary(kind, velocity, restore, radius)
+        self._chk(self.L.tfg_batch_set_boundary(self.b.h, self.sid, wall, C.byref(b)), "batch_set_boundary")
+
+    def set_boundary_potential(self, wall, t, pot):
+        ptr = pot.ptr if isinstance(pot, Potential) else pot
+        self._chk(self.L.tfg_batch_set_boundary_potential(self.b.h, self.sid, wall, t, ptr),
+                  "batch_set_boundary_potential")
+
     def load(self, x, v=None, type=None, radius=None, imass=None, flags=None, species=None, force_i=None):
         x = np.ascontiguousarray(x, np.float32)
         self.n = x.shape[0]
@@ -345,6 +362,12 @@ def setup_model(eng, w, keep=None, pot_cache=None):
         mean, std, dur = w.random_force
         for t in range(w.max_type):
             eng.set_random_force(t, mean, std, dur)
+    for (wall, kind, vel, restore, radius) in w.boundaries:
+        eng.set_boundary(wall, kind, vel, restore, radius)
+    for (wall, t, spec) in w.wall_pots:
+        p = _potential(spec, pot_cache)
+        pots.append(p)
+        eng.set_boundary_potential(wall, t, p.ptr)
     if w.bond_pot is not None:
         p = _potential(w.bond_pot, pot_cache)
         pots.append(p)
