@@ -285,13 +285,14 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def serve_sample(args, dev, count):
+def serve_sample(args, dev, count, rate=200.0):
     """A bounded sample of the served stream: the first `count` requests of the Poisson
-    stream, with their particles generated before the clock starts (client-side data)."""
+    stream at `rate` requests/s, with their particles generated before the clock starts
+    (client-side data)."""
     from tfg import configs
     from tfg.serving import Request, Server, summarize
     reqs = []
-    for r in configs.served_requests(count=count, seed=args.seed):
+    for r in configs.served_requests(count=count, rate=rate, seed=args.seed):
         reqs.append(Request(len(reqs), r["t"] - 0.0, configs.request_workload(r), r["steps"]))
     t_first = reqs[0].t_arrival
     for r in reqs:
@@ -302,6 +303,7 @@ def serve_sample(args, dev, count):
     s = summarize(done)
     s.update({"max_concurrent": srv.max_concurrent, "chunks": srv.chunks, "quantum": args.quantum,
               "max_particles_in_flight": args.serve_particles, "budget_bytes": 150 << 30,
+              "rate_per_s": rate,
               "sample": "first %d of the 10,000 requests (arrivals re-based to t=0)" % count})
     return s
 
@@ -389,7 +391,7 @@ def run_ensemble(args, rank, world, dev, dist):
              "how": "each simulation alone in its own engine (same kernels, CUDA graphs), one after another"}
 
     # end to end: the whole job through the C ABI with host arrays
-    E = args.e2e_steps
+    E = args.e2e_steps or ws[0].steps
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     host = [(pin(w.x), pin(w.type), pin(w.radius), pin(w.imass)) for w in ws]
     outs = []
@@ -447,6 +449,12 @@ def run_ensemble(args, rank, world, dev, dist):
                          "CPU restatement of the reference engine, %.1f s" % (
                              len(ws), max(1, len(ws) // 16), sum(w.n for w in sample), min(steps), max(steps), dt)}
     serving = serve_sample(args, dev, args.requests) if (rank == 0 and args.requests > 0) else None
+    if serving is not None and args.sustained_requests > 0:
+        # the same stream at an arrival rate the GPU sustains (about half its served capacity),
+        # so the latencies show service time rather than backlog
+        work = serving["particle_steps"] / serving["requests"]
+        rate = 0.5 * serving["achieved_particle_steps_per_s"] / work
+        serving["at_sustainable_rate"] = serve_sample(args, dev, args.sustained_requests, rate=rate)
     if rank == 0:
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
@@ -538,7 +546,7 @@ def run_single(args, rank, world, dev, dist):
     value = world * w.n * args.steps / (t_ms * 1e-3)
 
     # end to end: load from host arrays, run --e2e-steps steps, download
-    E = args.e2e_steps
+    E = args.e2e_steps or min(w.steps, 200)
     pin = lambda a: None if a is None else torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     hx, hv, ht, hr, hi, hs = (pin(a) for a in (w.x, w.v, w.type, w.radius, w.imass, w.species))
     e2e_eng = Engine(w.desc(device=dev))
@@ -605,7 +613,10 @@ def main():
     ap.add_argument("--workload", default="ensemble", choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="tfg", choices=["tfg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=100)
+    ap.add_argument("--e2e-steps", type=int, default=0,
+                    help="steps of the end-to-end job (0: the workload's own step count, 1,000 for the ensemble)")
+    ap.add_argument("--sustained-requests", type=int, default=40,
+                    help="served requests at a sustainable arrival rate (0: skip)")
     ap.add_argument("--n", type=int, default=0, help="scale a single-simulation workload to n particles")
     ap.add_argument("--relax", type=int, default=None, help="override the relaxation steps")
     ap.add_argument("--sims", type=int, default=256, help="simulations in the ensemble")
