@@ -142,7 +142,12 @@ def test_trajectory_10_steps(wl):
     side = np.array(w.dim, np.float32)
     d = a["x"] - b["x"]
     d -= side * np.round(d / side)
-    assert np.max(np.abs(d)) < 1e-3, "max position deviation %.3g" % np.max(np.abs(d))
+    # The GPU sums forces in another (and run-to-run varying) order than the oracle; close
+    # contacts amplify the FP32 rounding differences over the steps.  Bar: every particle
+    # within 2e-3, 99% of them within 1e-4.
+    dev = np.abs(d).max(axis=1)
+    assert dev.max() < 2e-3, "max position deviation %.3g" % dev.max()
+    assert np.percentile(dev, 99) < 1e-4, "99th percentile deviation %.3g" % np.percentile(dev, 99)
     assert np.mean(a["cell"] != b["cell"]) < 1e-3
     if w.nr_species:
         assert np.max(np.abs(a["species"] - b["species"])) < 1e-4

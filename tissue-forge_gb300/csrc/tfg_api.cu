@@ -43,13 +43,13 @@ int make_engine(int device, int max_type, int nspec, tfg_engine **out) {
     for (auto &p : eng->h_bpots) std::memset(&p, 0, sizeof(p));
     eng->h_btables.assign(kMaxBondSlots, std::vector<float>());
     int rc;
-    if ((rc = dalloc(eng, &eng->err, 1)) || (rc = dalloc(eng, &eng->overflow_count, 1)) ||
+    if ((rc = dalloc(eng, &eng->err, 1)) || (rc = dalloc(eng, &eng->overflow_count, 2)) ||
         (rc = dalloc(eng, &eng->bpots, kMaxBondSlots)) || (rc = dalloc(eng, &eng->stamps, 5))) {
         destroy(eng);
         return rc;
     }
     cudaMemset(eng->err, 0, sizeof(uint32_t));
-    cudaMemset(eng->overflow_count, 0, sizeof(int));
+    cudaMemset(eng->overflow_count, 0, 2 * sizeof(int));
     cudaMemset(eng->stamps, 0, sizeof(unsigned long long) * 5);
     if (cudaDeviceSynchronize() != cudaSuccess) {
         destroy(eng);

@@ -29,6 +29,7 @@ constexpr int kCapT = 160;          // staged particles per warp (table variants
 constexpr int kCapX = 104;          // staged particles per warp (DPD and flux variants)
 constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
 constexpr int kQ = 64;              // candidate ring queue entries per warp (power of two)
+constexpr int kGrab = 1;            // work items a warp takes from the shared counter at a time
 constexpr int kMaxSmemTable = 4096; // floats of potential table staged per CTA
 constexpr int kMaxSmemPots = 64;    // potential descriptors staged per CTA (all simulations)
 
@@ -61,7 +62,7 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 struct TileArgs {
     PairKernelArgs a;
     int *overflow_list;    // home cells handed to the overflow kernel
-    int *overflow_count;
+    int *overflow_count;   // [0] overflow cells, [1] work counter of the tiled pass
     int split;             // warps per home cell: the 14 tasks are divided into `split` groups
     int stage_floats;      // table floats and descriptors staged per CTA (TilePlan)
     int stage_pots;
@@ -333,11 +334,16 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
     Staged &S = L[wid];
     float epot = 0.f, vir = 0.f;
     int cur_rb = -1;
-    const int nwarps_total = gridDim.x * kWarps;
     const int per = 14 / T.split;
     const int nitems = a.ncells * T.split;
 
-    for (int item = blockIdx.x * kWarps + wid; item < nitems; item += nwarps_total) {
+    // warps take items (home cell x task group) from a shared counter, kGrab at a time, so
+    // that uneven cells (empty ones, droplet interiors) balance dynamically
+    int base = 0;
+    if (lane == 0) base = atomicAdd(T.overflow_count + 1, kGrab);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    for (; base < nitems;) {
+    for (int item = base; item < base + kGrab && item < nitems; item++) {
         const int home = item / T.split, grp = item - home * T.split;
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         if (nh == 0) continue;
@@ -506,6 +512,9 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
         }
         flush<kFlux, kSig>(a, S, 0, nh, lane);
         __syncwarp();
+    }
+    if (lane == 0) base = atomicAdd(T.overflow_count + 1, kGrab);
+    base = __shfl_sync(0xffffffffu, base, 0);
     }
     if (kSig) return;
     flush_red(a.red, cur_rb, epot, vir, lane);
@@ -686,7 +695,7 @@ void launch_pair_fluxonly(const PairKernelArgs &a, const TilePlan &plan, int *ov
     T.split = 1;
     T.stage_floats = plan.stage_floats;
     T.stage_pots = plan.stage_pots;
-    cudaMemsetAsync(overflow_count, 0, sizeof(int), s);
+    cudaMemsetAsync(overflow_count, 0, 2 * sizeof(int), s);
     if (a.n <= 0) return;
     launch_variant<false, true, false, false>(T, s, sms);
 }
@@ -709,7 +718,7 @@ void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overfl
     T.split = (split == 1 || split == 2 || split == 7 || split == 14) ? split : 1;
     T.stage_floats = plan.stage_floats;
     T.stage_pots = plan.stage_pots;
-    cudaMemsetAsync(overflow_count, 0, sizeof(int), s);
+    cudaMemsetAsync(overflow_count, 0, 2 * sizeof(int), s);
     if (a.n <= 0) return;
     const bool dpd = a.has_dpd, flux = a.nspec > 0 && a.has_flux;
     const bool dens = !(a.flags & TFG_ENGINE_NO_DENSITY);
