@@ -267,7 +267,9 @@ __device__ __forceinline__ void flush_red(double *red, int rb, float &epot, floa
 }
 
 template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __forceinline__ void stage(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane) {
+__device__ __forceinline__ void stage_body(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task,
+                                           int lane) {
+#pragma unroll 1
     for (int k = lane; k < n; k += 32) {
         const int g = g0 + k;
         const float4 ax = a.aux[g];
@@ -287,7 +289,8 @@ __device__ __forceinline__ void stage(const PairKernelArgs &a, ST &S, int base, 
 }
 
 template <bool kFlux, bool kSig, class ST>
-__device__ __forceinline__ void flush(const PairKernelArgs &a, ST &S, int b0, int b1, int lane) {
+__device__ __forceinline__ void flush_body(const PairKernelArgs &a, ST &S, int b0, int b1, int lane) {
+#pragma unroll 1
     for (int k = b0 + lane; k < b1; k += 32) {
         const float4 v = S.acc[k];
         const int g = S.gslot[k];
@@ -306,6 +309,28 @@ __device__ __forceinline__ void flush(const PairKernelArgs &a, ST &S, int b0, in
             if (q != 0.f) atomicAdd(&a.sq[g], q);
         }
     }
+}
+
+// Staging and flushing run once per segment, not per pair.  Out of line they keep the hot
+// candidate/evaluation loop of the table variants small in instruction cache; the DPD and
+// flux variants, whose evaluation is inlined once, run faster with them inline.
+template <bool kDPD, bool kFlux, bool kSig, class ST>
+__device__ __noinline__ void stage_call(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane) {
+    stage_body<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane);
+}
+template <bool kFlux, bool kSig, class ST>
+__device__ __noinline__ void flush_call(const PairKernelArgs &a, ST &S, int b0, int b1, int lane) {
+    flush_body<kFlux, kSig>(a, S, b0, b1, lane);
+}
+template <bool kDPD, bool kFlux, bool kSig, class ST>
+__device__ __forceinline__ void stage(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane) {
+    if constexpr (kDPD || kFlux) stage_body<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane);
+    else stage_call<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane);
+}
+template <bool kDPD, bool kFlux, bool kSig, class ST>
+__device__ __forceinline__ void flush(const PairKernelArgs &a, ST &S, int b0, int b1, int lane) {
+    if constexpr (kDPD || kFlux) flush_body<kFlux, kSig>(a, S, b0, b1, lane);
+    else flush_call<kFlux, kSig>(a, S, b0, b1, lane);
 }
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
@@ -390,6 +415,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
         // wall potentials of the home particles, once per home cell (runner_doself's
         // boundary_eval, tf_runner_dopair.cpp:594-596)
         if (!kSig && t0 == 13 && a.has_wall_pots && P.walls_active && !(kFlux && a.flux_sub >= 0)) {
+#pragma unroll 1
             for (int k = lane; k < nh; k += 32) {
                 const float4 p4 = S.pos[k];
                 const int g = S.gslot[k];
@@ -507,10 +533,10 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                 }
                 __syncwarp();
             }
-            flush<kFlux, kSig>(a, S, nh, end, lane);
+            flush<kDPD, kFlux, kSig>(a, S, nh, end, lane);
             __syncwarp();
         }
-        flush<kFlux, kSig>(a, S, 0, nh, lane);
+        flush<kDPD, kFlux, kSig>(a, S, 0, nh, lane);
         __syncwarp();
     }
     if (lane == 0) base = atomicAdd(T.overflow_count + 1, kGrab);
