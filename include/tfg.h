@@ -162,9 +162,23 @@ typedef struct tfg_engine_desc {
  *   used).  Without it the term is sigma*omega*xi/sqrt(dt) with xi ~ N(0,1) drawn from a
  *   Philox4x32-10 stream keyed on (seed, step, min id, max id).
  * TFG_ENGINE_NO_DENSITY: skip the number-density side output f[3]
- *   (tf_runner_dopair.cpp:175-177). */
+ *   (tf_runner_dopair.cpp:175-177).
+ * TFG_ENGINE_VERLET: the reference's engine_flag_verlet (tfEngine.h:74; engine_init
+ *   tfEngine.cpp:1749-1752).  Particles stay in their cells between rebuilds: a step
+ *   re-bins (space_shuffle_local) only when twice the largest displacement since the last
+ *   rebuild exceeds the skin min(h) - cutoff (engine_verlet_update, tfEngine.cpp:214-354),
+ *   and the integrator is the reference's Verlet branch (tf_engine_advance.cpp:367-427: no
+ *   velocity clamp, frozen mask, wall reflection, migration or flux integration; computed
+ *   volume 0).  The first step after a load, a boundary change or a change of a batch's
+ *   membership rebuilds.  The displacement is measured as the
+ *   reference's OpenMP branch measures it; its default branch discards it (the sum goes to
+ *   a shadowing int), so the reference itself never rebuilds after the first step.  On the
+ *   device, the rebuild step also records each home cell's interacting-pair candidates
+ *   within the skin radius, and the other steps evaluate those lists instead of testing
+ *   every candidate pair. */
 #define TFG_ENGINE_DPD_REFERENCE_RANDOM (1u << 0)
 #define TFG_ENGINE_NO_DENSITY           (1u << 1)
+#define TFG_ENGINE_VERLET               (1u << 2)
 
 /* ---- boundary conditions (BoundaryConditions, tfBoundaryConditions.h:39-261) ----
  * Walls: 0 left (x low), 1 right (x high), 2 front (y low), 3 back (y high), 4 bottom
@@ -283,6 +297,11 @@ TFG_API int tfg_download(tfg_engine *eng, float *x, float *xrel, int32_t *cell, 
                          float *density, float *species, float *q);
 TFG_API int tfg_get_reductions(tfg_engine *eng, tfg_reductions *out);
 
+/* Verlet state of simulation 0 (TFG_ENGINE_VERLET): rebuilds so far, including the first
+ * step's, and the largest displacement since the last rebuild as of the last step
+ * (space::maxdx, 0 on a rebuild step).  Either pointer may be NULL. */
+TFG_API int tfg_get_verlet(tfg_engine *eng, int64_t *rebuilds, float *maxdx);
+
 /* Per-step timing of the device phases of the last step, in milliseconds, from GPU
  * global-timer stamps written between the phases: [0] bin, [1] pair, [2] bonded,
  * [3] advance (-1 when no step has been timed). */
@@ -334,6 +353,7 @@ TFG_API int tfg_batch_get_count(const tfg_engine *eng, int sim, int *n);
 TFG_API int tfg_batch_download(tfg_engine *eng, int sim, float *x, float *xrel, int32_t *cell, float *v,
                                float *f, float *density, float *species, float *q);
 TFG_API int tfg_batch_get_reductions(tfg_engine *eng, int sim, tfg_reductions *out);
+TFG_API int tfg_batch_get_verlet(tfg_engine *eng, int sim, int64_t *rebuilds, float *maxdx);
 TFG_API int tfg_batch_set_boundary(tfg_engine *eng, int sim, int wall, const tfg_boundary *bc);
 TFG_API int tfg_batch_set_boundary_potential(tfg_engine *eng, int sim, int wall, int type, const tfg_potential *p);
 

@@ -73,6 +73,8 @@ def lib():
         L.tfo_download_fmag.argtypes = [E, C.POINTER(C.c_double)]
         L.tfo_get_reductions.argtypes = [E, C.POINTER(abi.Reductions)]
         L.tfo_get_stats.argtypes = [E, C.POINTER(C.c_int64)]
+        L.tfo_get_verlet.argtypes = [E, C.POINTER(C.c_int64), C.POINTER(C.c_float)]
+        L.tfo_verlet_hold.argtypes = [E]
         L.tfo_signature.argtypes = [E, abi.I_P, abi.U_P]
         L.tfo_enable_signature.argtypes = [E, C.c_int]
         L.tfo_record_pairs.argtypes = [E, C.c_int]
@@ -242,6 +244,16 @@ class OracleEngine:
         r = abi.Reductions()
         _chk(self.L.tfo_get_reductions(self.h, C.byref(r)), "reductions")
         return r
+
+    def verlet(self):
+        """(rebuilds so far, space::maxdx after the last step) in Verlet mode."""
+        nb, m = C.c_int64(), C.c_float()
+        _chk(self.L.tfo_get_verlet(self.h, C.byref(nb), C.byref(m)), "verlet")
+        return int(nb.value), float(m.value)
+
+    def verlet_hold(self):
+        """Take the current cells and positions as the last Verlet rebuild's."""
+        _chk(self.L.tfo_verlet_hold(self.h), "verlet_hold")
 
     def stats(self):
         s = (C.c_int64 * 3)()

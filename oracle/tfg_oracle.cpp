@@ -110,6 +110,7 @@ template <typename R> struct Part {
     float fi[3];        // force_i (external)
     float v[4];         // velocity; v[3] = inverse number density
     float x[4];         // cell-relative position
+    float ox[3];        // Verlet reference position (space_cell::oldx)
     float pf[3];        // persistent (random) force
     float imass, radius;
     int id, type;
@@ -185,6 +186,12 @@ template <typename R> struct Engine {
     std::vector<Pot<R>> wpots;   // 6 x max_type
     bool tasks_dirty = false;
     int nr_fluxsteps = 1;
+    // Verlet mode (engine_flag_verlet): skin, rebuild flag, space::maxdx, rebuild count
+    bool verlet = false;
+    float skin = 0.f;
+    bool verlet_rebuild = true;
+    float verlet_maxdx = 0.f;
+    int64_t verlet_rebuilds = 0;
     R epot_nonbond = 0, epot_bond = 0, epot_angle = 0;
     double kinetic = 0, virial = 0, computed_volume = 0;
     int64_t migrations = 0, straight_angles = 0;
@@ -330,6 +337,8 @@ template <typename R> static int init_space(Engine<R> &e, const tfg_engine_desc 
     // dt_flux = dt / nr_fluxsteps (tfSimulator.cpp:653), an FP32 division
     e.nr_fluxsteps = d->nr_fluxsteps > 0 ? d->nr_fluxsteps : 1;
     e.dt_flux = d->dt / (float)e.nr_fluxsteps;
+    e.verlet = (d->flags & TFG_ENGINE_VERLET) != 0;
+    e.skin = std::fmin(e.h[0], std::fmin(e.h[1], e.h[2])) - e.cutoff;   // tfEngine.cpp:231
     return TFG_OK;
 }
 
@@ -580,7 +589,7 @@ template <typename R> static void do_pair(Engine<R> &e, int ci0, int cj0, R &epo
     } else {
         float bias = std::sqrt(e.h[0] * e.h[0] + e.h[1] * e.h[1] + e.h[2] * e.h[2]);
         float dscale = (float)SHRT_MAX / (2 * bias);
-        int dmaxdist = 2 + dscale * (e.cutoff + 2 * 0.0f);
+        int dmaxdist = 2 + dscale * (e.cutoff + 2 * e.verlet_maxdx);   // tf_runner_dopair.cpp:115-117
         float nshift = std::sqrt(shift[0] * shift[0] + shift[1] * shift[1] + shift[2] * shift[2]);
         int dnshift = dscale * nshift;
         const unsigned *ip = &A.sortlist[(size_t)ni * sid];
@@ -905,7 +914,11 @@ static inline int axis_colour(int x, int n) {
 // This gives the reference runners' per-cell exclusion (tfRunner.cpp:204-380) with a
 // deterministic task order.
 template <typename R> static void nonbond(Engine<R> &e) {
-    par_for(e.nthreads, (size_t)e.ncells, 64, [&](size_t cid) { do_sort(e, (int)cid); });
+    // sort tasks run only while a Verlet rebuild is due (tfRunner.cpp:314; without the
+    // Verlet flag verlet_rebuild stays set); between rebuilds the windows of the last sort
+    // are widened by 2 maxdx
+    if (!e.verlet || e.verlet_rebuild)
+        par_for(e.nthreads, (size_t)e.ncells, 64, [&](size_t cid) { do_sort(e, (int)cid); });
     if (e.owned.empty()) {
         e.owned.assign(e.ncells, std::vector<int>());
         for (size_t k = 0; k < e.tasks.size(); k++) e.owned[e.tasks[k].i].push_back((int)k);
@@ -1135,13 +1148,73 @@ template <typename R> static void flux_substeps(Engine<R> &e) {
     }
 }
 
+// engine_verlet_update (tfEngine.cpp:214-354): unless a rebuild is already due, the largest
+// displacement since the last rebuild, measured as the OpenMP branch does (:239-252; the
+// default branch sums into a shadowing int and so always finds 0); rebuild when twice it
+// exceeds the skin, by re-binning (engine_shuffle) and storing the reference positions.
+template <typename R> static void verlet_update(Engine<R> &e) {
+    if (!e.verlet_rebuild) {
+        float m2 = 0.f;
+        for (auto &c : e.cells)
+            for (auto &p : c.parts) {
+                float dx = 0.0f;
+                for (int k = 0; k < 3; k++) {
+                    const float w = p.x[k] - p.ox[k];
+                    dx += w * w;
+                }
+                m2 = std::fmax(dx, m2);
+            }
+        const float m = std::sqrt(m2);
+        e.verlet_rebuild = 2.0 * m > e.skin;
+        e.verlet_maxdx = m;
+    }
+    if (e.verlet_rebuild) {
+        shuffle(e);
+        for (auto &c : e.cells)
+            for (auto &p : c.parts)
+                for (int k = 0; k < 3; k++) p.ox[k] = p.x[k];
+        e.verlet_maxdx = 0.f;
+        e.verlet_rebuilds++;
+    }
+}
+
+// The Verlet branch of engine_advance_forward_euler (tf_engine_advance.cpp:367-427): no
+// frozen mask, velocity clamp, wall reflection, migration or flux integration; the
+// computed volume sums the cells' values, which space_prepare zeroed.
+template <typename R> static int advance_verlet(Engine<R> &e) {
+    const float dt = e.dt;
+    for (auto &c : e.cells)
+        for (auto &p : c.parts) {
+            const float fx[3] = {(float)p.f[0], (float)p.f[1], (float)p.f[2]};
+            if (e.dyn[p.type] == TFG_NEWTONIAN) {
+                for (int k = 0; k < 3; k++) {
+                    p.v[k] += fx[k] * dt * p.imass;
+                    p.x[k] += p.v[k] * dt;
+                }
+            } else {
+                for (int k = 0; k < 3; k++) {
+                    p.v[k] = fx[k] * p.imass;
+                    p.x[k] += p.v[k] * dt;
+                }
+            }
+        }
+    e.migrations = 0;
+    e.computed_volume = 0;
+    return TFG_OK;
+}
+
 template <typename R> static int step(Engine<R> &e) {
     e.time += 1;
     kinetic(e);
     prepare(e);
-    shuffle(e);
+    if (e.verlet) verlet_update(e);
+    else shuffle(e);
     flux_substeps(e);
     force_all(e, true);
+    if (e.verlet) {
+        e.verlet_rebuild = false;   // engine_force, tfEngine.cpp:1539-1540
+        return advance_verlet(e);
+    }
     return advance(e);
 }
 
@@ -1182,6 +1255,9 @@ template <typename R> static int load_common(Engine<R> &e, int n, const float *v
         e.cells[c].parts.push_back(p);
     }
     e.time = 0;
+    e.verlet_rebuild = true;   // engine_start (tfEngine.cpp:1238-1263)
+    e.verlet_maxdx = 0.f;
+    e.verlet_rebuilds = 0;
     return TFG_OK;
 }
 
@@ -1302,6 +1378,7 @@ TFG_API int tfo_set_boundary(tfo_engine *eh, int wall, const tfg_boundary *bc) {
             }
         }
         build_tasks(e);
+        e.verlet_rebuild = true;
         return TFG_OK;
     };
     return DISPATCH(h, go);
@@ -1442,8 +1519,28 @@ TFG_API int tfo_force_only(tfo_engine *eh, int with_bonded) {
         e.time += 1;
         kinetic(e);
         prepare(e);
-        shuffle(e);
-        return force_all(e, with_bonded != 0);
+        if (e.verlet) verlet_update(e);
+        else shuffle(e);
+        const int rc = force_all(e, with_bonded != 0);
+        e.verlet_rebuild = false;
+        return rc;
+    };
+    return DISPATCH(h, go);
+}
+
+// Test hook (Verlet mode): take the current cells and positions as the last rebuild's, so
+// that the next step or force pass does not re-bin.  The sorted windows are only valid for
+// positions inside their cells; for others use brute-force pair enumeration (mode bit 2).
+TFG_API int tfo_verlet_hold(tfo_engine *eh) {
+    Handle *h = reinterpret_cast<Handle *>(eh);
+    auto go = [&](auto &e) {
+        for (auto &c : e.cells)
+            for (auto &p : c.parts)
+                for (int k = 0; k < 3; k++) p.ox[k] = p.x[k];
+        for (int cid = 0; cid < e.ncells; cid++) do_sort(e, cid);
+        e.verlet_rebuild = false;
+        e.verlet_maxdx = 0.f;
+        return TFG_OK;
     };
     return DISPATCH(h, go);
 }
@@ -1496,6 +1593,16 @@ TFG_API int tfo_get_reductions(tfo_engine *eh, tfg_reductions *out) {
         }
         out->steps = e.time;
         out->migrations = e.migrations;
+        return TFG_OK;
+    };
+    return DISPATCH(h, go);
+}
+
+TFG_API int tfo_get_verlet(tfo_engine *eh, int64_t *rebuilds, float *maxdx) {
+    Handle *h = reinterpret_cast<Handle *>(eh);
+    auto go = [&](auto &e) {
+        if (rebuilds) *rebuilds = e.verlet_rebuilds;
+        if (maxdx) *maxdx = e.verlet_maxdx;
         return TFG_OK;
     };
     return DISPATCH(h, go);

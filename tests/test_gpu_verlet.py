@@ -1,0 +1,109 @@
+"""Verlet mode on the GPU (TFG_ENGINE_VERLET) against the oracle's Verlet mode: rebuild
+decisions, the pair set with particles outside their cells (bit-exact), trajectories, and
+batches that mix Verlet and cell-list simulations."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import make_gpu, make_oracle, small_bonded, small_dpd
+from tfg import abi, configs
+from tfg.engine import Batch, Engine, setup_model
+
+pytestmark = pytest.mark.gpu
+
+
+def _relaxed(w, steps=200):
+    """`w` with its positions after `steps` overdamped cell-list steps under the reference's
+    displacement clamp.  The Verlet integrator has no clamp, so overlapping chain beads of
+    the generated start would fly apart."""
+    base = dataclasses.replace(w, flags=w.flags & ~abi.ENGINE_VERLET, dynamics=[abi.OVERDAMPED] * w.max_type)
+    o = make_oracle(base)
+    o.step(steps)
+    return dataclasses.replace(w, x=configs.in_box(o.download()["x"], w.dim[0]))
+
+
+WORKLOADS = {
+    # 4,000 particles, 5^3 cells of edge 4 (skin 1)
+    "cell_sorting": lambda: configs.verlet(configs.cell_sorting(random_force=(0.0, 2.0, 1)), skin=0.3),
+    # 4,000 DPD particles with flux, 8^3 cells of edge 1.5 (skin 0.5)
+    "dpd": lambda: configs.verlet(small_dpd(), skin=0.4),
+    # 8,000 LJ particles in chains, relaxed first (200 steps); skin 0.75
+    "bonded": lambda: _relaxed(configs.verlet(small_bonded(), skin=0.3)),
+}
+
+
+@pytest.fixture(params=sorted(WORKLOADS))
+def wl(request):
+    return request.param, WORKLOADS[request.param]()
+
+
+def _dev(a, b, dim):
+    side = np.array(dim, np.float32)
+    d = a - b
+    d -= side * np.round(d / side)
+    return np.abs(d).max(axis=1)
+
+
+def test_trajectory_and_rebuilds_match_oracle(wl):
+    name, w = wl
+    g = make_gpu(w)
+    o = make_oracle(w)
+    for _ in range(12):
+        g.step(1)
+        o.step(1)
+        assert g.verlet()[0] == o.verlet()[0], name
+    a, b = g.download(), o.download()
+    # same bar as the cell-list trajectories: summation order differs from the oracle's
+    dev = _dev(a["x"], b["x"], w.dim)
+    assert dev.max() < 2e-3, "max position deviation %.3g" % dev.max()
+    assert np.percentile(dev, 99) < 1e-4
+    assert np.array_equal(a["cell"], b["cell"])
+    if w.nr_species:
+        assert np.max(np.abs(a["species"] - b["species"])) < 1e-4
+    rb, maxdx = g.verlet()
+    assert abs(maxdx - o.verlet()[1]) < 1e-4
+
+
+def test_pair_set_with_particles_outside_their_cells_bitexact(wl):
+    name, w = wl
+    o = make_oracle(w)
+    o.step(8)
+    d = o.download()
+    h = np.array([dm / c for dm, c in zip(w.dim, w.cells)], np.float32)
+    assert np.any((d["xrel"] < 0) | (d["xrel"] >= h)), "no particle outside its cell"
+    args = dict(v=d["v"], type=w.type, radius=w.radius, imass=w.imass,
+                species=d["species"] if w.nr_species else None)
+    g = make_gpu(w)
+    g.load_binned(d["cell"], d["xrel"], **args)
+    gc, gh = g.pair_signature()
+    r = O.OracleEngine(w.desc(), O.MODE_BRUTE, 1)
+    r._keep = setup_model(r, w)
+    r.load_binned(d["cell"], d["xrel"], **args)
+    r.verlet_hold()
+    r.force_only()
+    rc, rh = r.signature()
+    assert np.array_equal(gc, rc), "pair counts differ for %d particles" % int((gc != rc).sum())
+    assert np.array_equal(gh, rh)
+
+
+def test_batch_mixing_verlet_and_cell_list_members_equals_alone():
+    ws = [configs.verlet(configs.cell_sorting(n=2500, side=17.0, seed=21, random_force=(0.0, 2.0, 1)), skin=0.3),
+          configs.cell_sorting(n=900, side=12.5, depth_ab=1.7, seed=22),
+          configs.verlet(configs.cell_sorting(n=6000, side=22.9, seed=23, random_force=(0.0, 2.0, 1)), skin=0.5)]
+    b = Batch(ws[0].max_type, ws[0].nr_species)
+    sims = []
+    for w in ws:
+        s = b.add_sim(w.desc())
+        b._keep.extend(setup_model(s, w))
+        sims.append(s)
+    b.step(10)
+    for w, s in zip(ws, sims):
+        g = make_gpu(w)
+        g.step(10)
+        a, r = s.download(), g.download()
+        assert np.array_equal(a["cell"], r["cell"]), w.name
+        assert _dev(a["x"], r["x"], w.dim).max() < 1e-3, w.name
+        if w.flags:
+            assert s.verlet()[0] == g.verlet()[0] > 1, w.name

@@ -476,6 +476,14 @@ TFG_API int tfg_batch_set_boundary_potential(tfg_engine *eng, int sim, int wall,
 TFG_API int tfg_batch_get_reductions(tfg_engine *eng, int sim, tfg_reductions *out) {
     return reductions_sim(eng, sim, out);
 }
+TFG_API int tfg_get_verlet(tfg_engine *eng, int64_t *rebuilds, float *maxdx) {
+    if (!eng) return TFG_E_INVAL;
+    return verlet_sim(eng, 0, rebuilds, maxdx);
+}
+TFG_API int tfg_batch_get_verlet(tfg_engine *eng, int sim, int64_t *rebuilds, float *maxdx) {
+    if (!eng) return TFG_E_INVAL;
+    return verlet_sim(eng, sim, rebuilds, maxdx);
+}
 
 TFG_API int tfg_get_phase_ms(tfg_engine *eng, float ms[4]) {
     if (!eng || !ms) return TFG_E_INVAL;

@@ -89,6 +89,14 @@ struct SimParams {
     float4 wall_vel[6];      // wall velocity; w = restore
     float wall_radius[6];
     int32_t wpot_base;       // (wall 0, type 0) in the wall-potential array; walls x types
+    // Verlet mode (TFG_ENGINE_VERLET; engine_verlet_update, tfEngine.cpp:214-354).  The
+    // device fields are written by k_tick and k_advance; the host writes 2 to
+    // verlet_rebuild to force a rebuild at the next step.
+    float skin;              // min(h) - cutoff
+    int32_t verlet_rebuild;  // device: this step re-bins and rebuilds the pair lists
+    uint32_t verlet_maxdx2;  // device: max |x - oldx|^2 after the last advance (float bits)
+    float verlet_maxdx;      // device: largest displacement at the last check (0 on a rebuild)
+    int64_t verlet_rebuilds; // device: rebuilds so far
 };
 
 // Is wall w of this simulation active and is cell location (a, b, c) on it?

@@ -128,6 +128,25 @@ int relayout(tfg_engine *eng) {
     std::vector<int> order;
     for (int k = 0; k < (int)eng->sims.size(); k++)
         if (eng->sims[k].live && eng->sims[k].loaded) order.push_back(k);
+    // Verlet state kept on the device (rebuild count, last displacement) survives the
+    // re-upload of the parameters; every Verlet simulation rebuilds at the next step.
+    bool any_verlet = false;
+    for (int k : order) any_verlet |= (eng->sims[k].P.flags & TFG_ENGINE_VERLET) != 0;
+    if (any_verlet && eng->sims_dev && !eng->order.empty()) {
+        std::vector<SimParams> dev(eng->order.size());
+        CK(cudaMemcpyAsync(dev.data(), eng->sims_dev, sizeof(SimParams) * dev.size(), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        for (size_t q = 0; q < eng->order.size(); q++) {
+            SimHost &S = eng->sims[eng->order[q]];
+            if (!S.live || S.pending) continue;
+            S.P.verlet_rebuilds = dev[q].verlet_rebuilds;
+            S.P.verlet_maxdx = dev[q].verlet_maxdx;
+        }
+    }
+    for (int k : order) {
+        eng->sims[k].P.verlet_rebuild = 2;
+        eng->sims[k].P.verlet_maxdx2 = 0u;
+    }
     int N = 0, C = 0, NA = 0, NB = 0;
     std::vector<int> old_slot(order.size()), old_cell(order.size());
     std::vector<bool> was_in(order.size());
@@ -187,6 +206,11 @@ int relayout(tfg_engine *eng) {
         eng->cap = new_cap;
     } else {
         eng->cur ^= 1;
+    }
+    if (any_verlet && eng->oldx_cap < eng->cap) {
+        int r2 = dalloc(eng, &eng->oldx, eng->cap);
+        if (r2) return r2;
+        eng->oldx_cap = eng->cap;
     }
     // per-simulation parameters with device pointers to the concatenated cell origins
     size_t norig = 0;
@@ -547,6 +571,9 @@ int add_sim(tfg_engine *eng, const tfg_engine_desc *d, int *out) {
     P.dt_flux = P.dt / (float)P.nr_fluxsteps;   // tfSimulator.cpp:653
     P.flags = d->flags;
     P.seed = d->seed;
+    // engine_verlet_update (tfEngine.cpp:231): skin = min(h) - cutoff, in FP32
+    P.skin = std::fmin(P.h[0], std::fmin(P.h[1], P.h[2])) - P.cutoff;
+    P.verlet_rebuild = 2;
     S.maxc = std::max(P.cdim[0], std::max(P.cdim[1], P.cdim[2]));
     S.orig.assign((size_t)3 * S.maxc, 0.f);
     for (int k = 0; k < 3; k++)
@@ -612,6 +639,8 @@ int load_sim(tfg_engine *eng, int sim, int n, const float *xg, const int32_t *ce
     S.loaded = true;
     S.pending = true;
     S.time = 0;
+    S.P.verlet_rebuilds = 0;
+    S.P.verlet_maxdx = 0.f;
     eng->layout_dirty = true;
     return TFG_OK;
 }
@@ -637,6 +666,7 @@ int bin(tfg_engine *eng, int shuffle) {
     b.slot_of_id = eng->slot_of_id;
     b.rforce = eng->rforce;
     b.force = eng->force;
+    b.oldx = eng->oldx;
     if (b.ncells == 0) return TFG_OK;
     launch_bin(b, eng->stream);
     eng->cur ^= 1;
@@ -760,7 +790,7 @@ int enqueue_step(tfg_engine *eng, bool advance, bool timed) {
     if (rc) return rc;
     if (advance)
         launch_advance(eng->n, eng->cap, eng->nspec, eng->sims_dev, eng->cell_sim, eng->A[eng->cur], eng->force,
-                       eng->type_mass, eng->type_dyn, eng->species_flags, eng->red, eng->err, s);
+                       eng->type_mass, eng->type_dyn, eng->species_flags, eng->oldx, eng->red, eng->err, s);
     if (timed) launch_stamp(eng->stamps, 4, s);
     return check_launch(eng);
 }
@@ -933,6 +963,24 @@ int reductions_sim(tfg_engine *eng, int sim, tfg_reductions *out) {
     return read_err(eng);
 }
 
+int verlet_sim(tfg_engine *eng, int sim, int64_t *rebuilds, float *maxdx) {
+    int rc = sim_check(eng, sim);
+    if (rc) return rc;
+    SimHost &S = eng->sims[sim];
+    SimParams P = S.P;
+    if (S.in_arena && eng->sims_dev) {
+        const auto it = std::find(eng->order.begin(), eng->order.end(), sim);
+        if (it != eng->order.end()) {
+            CK(cudaMemcpyAsync(&P, eng->sims_dev + (it - eng->order.begin()), sizeof(SimParams),
+                               cudaMemcpyDeviceToHost, eng->stream));
+            CK(cudaStreamSynchronize(eng->stream));
+        }
+    }
+    if (rebuilds) *rebuilds = P.verlet_rebuilds;
+    if (maxdx) *maxdx = P.verlet_maxdx;
+    return read_err(eng);
+}
+
 void destroy(tfg_engine *eng) {
     if (eng->stream) cudaStreamSynchronize(eng->stream);
     drop_graphs(eng);
@@ -941,7 +989,7 @@ void destroy(tfg_engine *eng) {
                     eng->slot_of_id, eng->scan_sums, eng->cell_sim, eng->overflow_list, eng->overflow_count,
                     eng->sims_dev, eng->corig, eng->pots, eng->blob, eng->fluxes, eng->rforce, eng->type_mass,
                     eng->type_dyn, eng->species_flags, eng->bonds, eng->bond_slot, eng->angles, eng->bpots,
-                    eng->bblob, eng->red, eng->err};
+                    eng->bblob, eng->red, eng->err, eng->oldx};
     for (void *p : bufs) cudaFree(p);
     for (int k = 0; k < 5; k++)
         if (eng->ev[k]) cudaEventDestroy(eng->ev[k]);

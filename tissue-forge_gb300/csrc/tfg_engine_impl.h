@@ -54,6 +54,8 @@ struct tfg_engine {
     int n = 0, cap = 0, ncells = 0, cells_cap = 0, cur = 0;
     tfg::ParticleArrays A[2];
     float4 *force = nullptr;
+    float4 *oldx = nullptr;          // Verlet reference positions by slot
+    int oldx_cap = 0;
     int32_t *count = nullptr, *start = nullptr, *lidx = nullptr, *tmp_id = nullptr, *tmp_src = nullptr,
             *dest = nullptr, *slot_of_id = nullptr, *scan_sums = nullptr, *cell_sim = nullptr;
     int *overflow_list = nullptr, *overflow_count = nullptr;
@@ -155,6 +157,7 @@ int load_sim(tfg_engine *eng, int sim, int n, const float *xg, const int32_t *ce
 int download_sim(tfg_engine *eng, int sim, float *x, float *xrel, int32_t *cell, float *v, float *f, float *dens,
                  float *species, float *q);
 int reductions_sim(tfg_engine *eng, int sim, tfg_reductions *out);
+int verlet_sim(tfg_engine *eng, int sim, int64_t *rebuilds, float *maxdx);
 int set_boundary_sim(tfg_engine *eng, int sim, int wall, const tfg_boundary *bc);
 int set_boundary_potential_sim(tfg_engine *eng, int sim, int wall, int type, const tfg_potential *p);
 void resolve_boundaries(SimHost &S);   // periodicity and wall flags into S.P

@@ -57,9 +57,26 @@ __global__ void k_stamp(unsigned long long *t, int k) {
     t[k] = v;
 }
 
+// time += 1 (engine_step, tfEngine.cpp:1387) and, in Verlet mode, the rebuild decision of
+// engine_verlet_update (tfEngine.cpp:234-290): rebuild when 2 * maxdx > skin, maxdx being
+// the largest displacement since the last rebuild, measured after the previous advance.
 __global__ void k_tick(int nsims, SimParams *sims) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nsims) sims[k].time += 1;
+    if (k >= nsims) return;
+    SimParams &P = sims[k];
+    P.time += 1;
+    if (P.flags & TFG_ENGINE_VERLET) {
+        int rb = P.verlet_rebuild == 2;
+        float m = 0.f;
+        if (!rb) {
+            m = __fsqrt_rn(__uint_as_float(P.verlet_maxdx2));
+            rb = __fmul_rn(2.0f, m) > P.skin;
+        }
+        P.verlet_maxdx = rb ? 0.f : m;
+        P.verlet_rebuild = rb;
+        P.verlet_maxdx2 = 0u;
+        if (rb) P.verlet_rebuilds += 1;
+    }
 }
 
 // space_setpartp (tfSpace.cpp:432-475) for one simulation's particles, written to arena
@@ -119,6 +136,11 @@ __global__ void k_bin_count(int n, const SimParams *sims, const int32_t *cell_si
     int c = cell[i];
     if (shuffle) {
         const SimParams &P = sims[cell_sim[c]];
+        // Verlet mode re-bins only on rebuild steps (engine_verlet_update -> engine_shuffle)
+        if ((P.flags & TFG_ENGINE_VERLET) && !P.verlet_rebuild) {
+            lidx[i] = atomicAdd(&count[c], 1);
+            return;
+        }
         float4 p = pos[i];
         int d0 = (p.x >= P.h[0]) - (p.x < 0.f);
         int d1 = (p.y >= P.h[1]) - (p.y < 0.f);
@@ -230,7 +252,7 @@ __global__ void k_rank(int ncells, const int32_t *start, const int32_t *tmp_id, 
 
 __global__ void k_scatter(int n, int cap, int nspec, const int32_t *dest, ParticleArrays src, ParticleArrays dst,
                           int32_t *slot_of_id, const SimParams *sims, const int32_t *cell_sim, const float4 *rforce,
-                          float4 *force) {
+                          float4 *force, float4 *oldx) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int d = dest[i];
@@ -261,6 +283,8 @@ __global__ void k_scatter(int n, int cap, int nspec, const int32_t *dest, Partic
         force[d] = make_float4(fe.x, fe.y, fe.z, P.self_density);
     }
     dst.pos[d] = p;
+    // Verlet reference positions, stored after the rebuild's re-binning (tfEngine.cpp:308-335)
+    if (oldx && (P.flags & TFG_ENGINE_VERLET) && P.verlet_rebuild) oldx[d] = make_float4(p.x, p.y, p.z, 0.f);
     dst.vel[d] = src.vel[i];
     dst.aux[d] = ax;
     dst.fext[d] = fe;
@@ -399,17 +423,38 @@ __global__ void k_angles(int na, const SimParams *sims, const int32_t *cell_sim,
     keyed_add(red, rb, RED_EPOT_ANGLE, epot);
 }
 
+// Verlet mode: the integrator branch of engine_advance_forward_euler for Verlet lists
+// (tf_engine_advance.cpp:367-427), plus the squared displacement from the reference
+// position that engine_verlet_update takes the maximum of (tfEngine.cpp:239-252).
+__device__ __forceinline__ float advance_verlet(const SimParams &P, bool newtonian, const float4 &f, float imass,
+                                                float4 &p, float4 &v, const float4 &ox) {
+    const float dt = P.dt;
+    const float fv[3] = {f.x, f.y, f.z};
+    float x[3] = {p.x, p.y, p.z}, vv[3] = {v.x, v.y, v.z};
+    for (int k = 0; k < 3; k++) {
+        if (newtonian) vv[k] = __fadd_rn(vv[k], __fmul_rn(__fmul_rn(fv[k], dt), imass));
+        else vv[k] = __fmul_rn(fv[k], imass);
+        x[k] = __fadd_rn(x[k], __fmul_rn(vv[k], dt));
+    }
+    p = make_float4(x[0], x[1], x[2], p.w);
+    v = make_float4(vv[0], vv[1], vv[2], v.w);
+    const float w0 = __fsub_rn(x[0], ox.x), w1 = __fsub_rn(x[1], ox.y), w2 = __fsub_rn(x[2], ox.z);
+    return __fadd_rn(__fadd_rn(__fmul_rn(w0, w0), __fmul_rn(w1, w1)), __fmul_rn(w2, w2));
+}
+
 // cell_advance_forward_euler + Fluxes_integrate; one thread per particle.
-__global__ void k_advance(int n, int cap, int nspec, const SimParams *sims, const int32_t *cell_sim, float4 *pos,
+__global__ void k_advance(int n, int cap, int nspec, SimParams *sims, const int32_t *cell_sim, float4 *pos,
                           float4 *vel, const float4 *aux, const float4 *force, int32_t *cell, float *sval, float *sq,
-                          const float *type_mass, const int32_t *type_dyn, const uint32_t *species_flags, double *red,
-                          uint32_t *err) {
+                          const float *type_mass, const int32_t *type_dyn, const uint32_t *species_flags,
+                          const float4 *oldx, double *red, uint32_t *err) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     float ke = 0.f, vol = 0.f, mig = 0.f;
     float stot[kMaxSpecies];
 #pragma unroll
     for (int s = 0; s < kMaxSpecies; s++) stot[s] = 0.f;
     int rb = -1;
+    int vsim = -1;          // Verlet simulation of this particle
+    uint32_t dx2 = 0u;      // its squared displacement (float bits)
     if (i < n) {
         const int c0 = cell[i];
         const SimParams &P = sims[cell_sim[c0]];
@@ -422,6 +467,16 @@ __global__ void k_advance(int n, int cap, int nspec, const SimParams *sims, cons
         const float imass = ax.y;
         ke = 0.5f * type_mass[P.type_base + type] * (v.x * v.x + v.y * v.y + v.z * v.z);
         bool migrated = false;
+        if (P.flags & TFG_ENGINE_VERLET) {
+            const float d2 = advance_verlet(P, type_dyn[P.type_base + type] == TFG_NEWTONIAN, f, imass, p, v, oldx[i]);
+            if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(err, ERR_NAN);
+            pos[i] = p;
+            vel[i] = v;
+            vsim = cell_sim[c0];
+            dx2 = __float_as_uint(d2);
+            for (int s = 0; s < nspec; s++) stot[s] = sval[s * cap + i];
+            goto reduce;
+        }
         const bool frozen_all = (flags & TFG_PARTICLE_FROZEN_X) && (flags & TFG_PARTICLE_FROZEN_Y) &&
                                 (flags & TFG_PARTICLE_FROZEN_Z);
         if (!frozen_all) {
@@ -508,6 +563,18 @@ __global__ void k_advance(int n, int cap, int nspec, const SimParams *sims, cons
                 sq[s * cap + i] = 0.f;
             }
             stot[s] = sv;
+        }
+    }
+reduce:
+    {
+        // largest displacement per Verlet simulation: one atomic per warp when the warp's
+        // particles share a simulation
+        const int first = __shfl_sync(0xffffffffu, vsim, 0);
+        if (__all_sync(0xffffffffu, vsim == first)) {
+            const uint32_t m = __reduce_max_sync(0xffffffffu, dx2);
+            if (first >= 0 && (threadIdx.x & 31) == 0) atomicMax(&sims[first].verlet_maxdx2, m);
+        } else if (vsim >= 0) {
+            atomicMax(&sims[vsim].verlet_maxdx2, dx2);
         }
     }
     keyed_add(red, rb, RED_KINETIC, ke);
@@ -601,7 +668,7 @@ void launch_bin(const BinArgs &b, cudaStream_t s) {
         k_rank<<<nblk((long long)b.ncells * 32, kThreads), kThreads, 0, s>>>(b.ncells, b.start, b.tmp_id, b.tmp_src,
                                                                              b.dest);
         k_scatter<<<nblk(b.n, kThreads), kThreads, 0, s>>>(b.n, b.cap, b.nspec, b.dest, b.src, b.dst, b.slot_of_id,
-                                                          b.sims, b.cell_sim, b.rforce, b.force);
+                                                          b.sims, b.cell_sim, b.rforce, b.force, b.oldx);
     }
 }
 
@@ -621,13 +688,13 @@ void launch_angles(int na, const SimParams *sims, const int32_t *cell_sim, const
                                                         force, red);
 }
 
-void launch_advance(int n, int cap, int nspec, const SimParams *sims, const int32_t *cell_sim,
+void launch_advance(int n, int cap, int nspec, SimParams *sims, const int32_t *cell_sim,
                     const ParticleArrays &A, const float4 *force, const float *type_mass, const int32_t *type_dyn,
-                    const uint32_t *species_flags, double *red, uint32_t *err, cudaStream_t s) {
+                    const uint32_t *species_flags, const float4 *oldx, double *red, uint32_t *err, cudaStream_t s) {
     if (n > 0)
         k_advance<<<nblk(n, kThreads), kThreads, 0, s>>>(n, cap, nspec, sims, cell_sim, A.pos, A.vel, A.aux, force,
-                                                        A.cell, A.sval, A.sq, type_mass, type_dyn, species_flags, red,
-                                                        err);
+                                                        A.cell, A.sval, A.sq, type_mass, type_dyn, species_flags, oldx,
+                                                        red, err);
 }
 
 void launch_flux_integrate(int n, int cap, int nspec, int sub, const SimParams *sims, const int32_t *cell_sim,

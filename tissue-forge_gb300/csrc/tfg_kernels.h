@@ -18,6 +18,7 @@ struct BinArgs {
     int32_t *count, *start, *lidx, *tmp_id, *tmp_src, *dest, *scan_sums, *slot_of_id;
     const float4 *rforce;
     float4 *force;
+    float4 *oldx;   // Verlet reference positions by slot (written on rebuild steps), or null
 };
 
 void launch_tick(int nsims, SimParams *sims, cudaStream_t s);
@@ -36,9 +37,9 @@ void launch_bonds(int nb, const SimParams *sims, const int32_t *cell_sim, const 
 void launch_angles(int na, const SimParams *sims, const int32_t *cell_sim, const int4 *angles, const PotDev *bpots,
                    const float *bblob, const int32_t *slot_of_id, const float4 *pos, const int32_t *cell,
                    float4 *force, double *red, cudaStream_t s);
-void launch_advance(int n, int cap, int nspec, const SimParams *sims, const int32_t *cell_sim,
+void launch_advance(int n, int cap, int nspec, SimParams *sims, const int32_t *cell_sim,
                     const ParticleArrays &A, const float4 *force, const float *type_mass, const int32_t *type_dyn,
-                    const uint32_t *species_flags, double *red, uint32_t *err, cudaStream_t s);
+                    const uint32_t *species_flags, const float4 *oldx, double *red, uint32_t *err, cudaStream_t s);
 // Fluxes_integrate of flux substep `sub` over every particle of the simulations that have
 // that substep (tf_engine_advance.cpp:314-323, tfFlux.cpp:175-202).
 void launch_flux_integrate(int n, int cap, int nspec, int sub, const SimParams *sims, const int32_t *cell_sim,

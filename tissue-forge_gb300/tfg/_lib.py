@@ -56,6 +56,7 @@ def lib():
     L.tfg_get_count.argtypes = [E, C.POINTER(C.c_int)]
     L.tfg_download.argtypes = [E, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P]
     L.tfg_get_reductions.argtypes = [E, C.POINTER(abi.Reductions)]
+    L.tfg_get_verlet.argtypes = [E, C.POINTER(C.c_int64), C.POINTER(C.c_float)]
     L.tfg_get_phase_ms.argtypes = [E, C.POINTER(C.c_float)]
     L.tfg_set_phase_timing.argtypes = [E, C.c_int]
     L.tfg_probe_fp32_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]
@@ -85,5 +86,6 @@ def lib():
     L.tfg_batch_download.argtypes = [E, C.c_int, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P,
                                      abi.F_P]
     L.tfg_batch_get_reductions.argtypes = [E, C.c_int, C.POINTER(abi.Reductions)]
+    L.tfg_batch_get_verlet.argtypes = [E, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_float)]
     _lib = L
     return L

@@ -53,6 +53,7 @@ PARTICLE_FROZEN_Z = 1 << 5
 # engine flags (tfg_engine_desc.flags)
 ENGINE_DPD_REFERENCE_RANDOM = 1 << 0
 ENGINE_NO_DENSITY = 1 << 1
+ENGINE_VERLET = 1 << 2
 
 
 class Potential(C.Structure):

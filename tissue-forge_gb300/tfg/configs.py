@@ -226,3 +226,14 @@ def request_workload(req):
     scale = (n / 100_000) ** (1.0 / 3.0)
     side = max(40.0 * scale, 8.0)
     return dpd_droplets(n=n, side=side, radius=12.0 * scale, steps=req["steps"], seed=50_000 + req["seed"])
+
+
+def verlet(w, skin=0.2):
+    """`w` in Verlet mode (TFG_ENGINE_VERLET) on a coarser grid whose cell edge is at least
+    (1 + skin) * cutoff: the reference's skin is the slack min(h) - cutoff of the cell grid
+    (engine_verlet_update, tfEngine.cpp:231), so a Verlet run needs cells larger than the
+    cutoff."""
+    import dataclasses
+    cells = tuple(max(3, int(math.floor(d / (w.cutoff * (1.0 + skin))))) for d in w.dim)
+    return dataclasses.replace(w, cells=cells, flags=w.flags | abi.ENGINE_VERLET,
+                               name=w.name + "_verlet")

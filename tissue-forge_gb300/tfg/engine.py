@@ -181,6 +181,12 @@ class Engine:
         self._chk(self.L.tfg_get_reductions(self.h, C.byref(r)), "get_reductions")
         return r
 
+    def verlet(self):
+        """(rebuilds so far, largest displacement since the last rebuild) in Verlet mode."""
+        nb, m = C.c_int64(), C.c_float()
+        self._chk(self.L.tfg_get_verlet(self.h, C.byref(nb), C.byref(m)), "get_verlet")
+        return int(nb.value), float(m.value)
+
     def set_phase_timing(self, enable):
         self._chk(self.L.tfg_set_phase_timing(self.h, 1 if enable else 0), "set_phase_timing")
 
@@ -332,6 +338,11 @@ class Sim:
         r = abi.Reductions()
         self._chk(self.L.tfg_batch_get_reductions(self.b.h, self.sid, C.byref(r)), "batch_get_reductions")
         return r
+
+    def verlet(self):
+        nb, m = C.c_int64(), C.c_float()
+        self._chk(self.L.tfg_batch_get_verlet(self.b.h, self.sid, C.byref(nb), C.byref(m)), "batch_get_verlet")
+        return int(nb.value), float(m.value)
 
 
 def _potential(spec, cache):
