@@ -274,6 +274,11 @@ TFG_API int tfg_query(tfg_engine *eng, int *idle);
  * split or stream one step runs eagerly, and the following steps replay a captured
  * single-step graph (one per particle-buffer parity), phase events included. */
 TFG_API int tfg_set_graphs(tfg_engine *eng, int enable);
+/* Pair lists for simulations in Verlet mode (default on): the tiled pass records each home
+ * cell's pairs within the list radius at a rebuild and evaluates those lists until the
+ * next one; off, every step tests all candidate pairs of the cell stencil.  The pair set
+ * is the same either way. */
+TFG_API int tfg_set_pair_lists(tfg_engine *eng, int enable);
 /* Autotune the nonbonded pass's work split (warps per home cell: 1, 2, 7 or 14) by timing
  * each choice on the current state; the state is left unchanged.  tfg_step and
  * tfg_force_only run it on their first call; tfg_set_split fixes the split instead.
@@ -284,8 +289,9 @@ TFG_API int tfg_set_split(tfg_engine *eng, int split);
 /* Pair-set signature of the current binned state, per particle id: the number of
  * partners with r2 <= cutoff^2 and the wrap-around sum of a 32-bit mix of their ids.
  * It runs the pair pass's own stencil walk and pair decision (no forces).  Call it after
- * tfg_force_only to describe the pair set that pass used.  Verification hook; the
- * reference has no counterpart. */
+ * tfg_force_only to describe the pair set that pass used.  A simulation in Verlet mode
+ * that did not rebuild at its last step is walked through its pair lists, as its next
+ * force pass would be.  Verification hook; the reference has no counterpart. */
 TFG_API int tfg_pair_signature(tfg_engine *eng, int32_t *count, uint32_t *hash);
 
 TFG_API int tfg_get_count(const tfg_engine *eng, int *n);

@@ -107,3 +107,83 @@ def test_batch_mixing_verlet_and_cell_list_members_equals_alone():
         assert _dev(a["x"], r["x"], w.dim).max() < 1e-3, w.name
         if w.flags:
             assert s.verlet()[0] == g.verlet()[0] > 1, w.name
+
+
+def _held_signature(w, d):
+    """Oracle pair signature (brute force) of a binned state taken as the last rebuild's."""
+    r = O.OracleEngine(w.desc(), O.MODE_BRUTE, 1)
+    r._keep = setup_model(r, w)
+    r.load_binned(d["cell"], d["xrel"], v=d["v"], type=w.type, radius=w.radius, imass=w.imass,
+                  species=d["species"] if w.nr_species else None)
+    r.verlet_hold()
+    r.force_only()
+    return r.signature()
+
+
+def _walk_and_compare(g, w, steps, on_step=None):
+    """Step `g`; whenever the next step will not rebuild (twice the displacement since the
+    last rebuild within 0.9 skin), compare its pair signature, walked through the lists, with
+    the oracle's brute-force signature of the same state.  Returns the number compared."""
+    skin = min(dm / c for dm, c in zip(w.dim, w.cells)) - w.cutoff
+    side = np.array(w.dim, np.float64)
+    x_in = g.download()["x"].astype(np.float64)
+    ref = None
+    checked = nb = 0
+    for k in range(steps):
+        if on_step:
+            on_step(k)
+        g.step(1)
+        nb1 = g.verlet()[0]
+        if nb1 > nb:
+            ref = x_in            # this step re-binned the positions that entered it
+        nb = nb1
+        d = g.download()
+        x_in = d["x"].astype(np.float64)
+        dd = x_in - ref
+        dd -= side * np.round(dd / side)
+        if 2.0 * np.max(np.linalg.norm(dd, axis=1)) > 0.9 * skin:
+            continue              # the next step rebuilds
+        gc, gh = g.pair_signature()
+        rc, rh = _held_signature(w, d)
+        assert np.array_equal(gc, rc), "pair counts differ for %d particles" % int((gc != rc).sum())
+        assert np.array_equal(gh, rh)
+        checked += 1
+    return checked
+
+
+@pytest.mark.parametrize("name", ["cell_sorting", "bonded"])
+def test_pair_list_walk_bitexact(name):
+    """Between rebuilds the table variants evaluate the pair lists recorded at the last
+    rebuild.  Walked at the current positions while twice the displacement since that
+    rebuild is within the skin, the lists give exactly the pairs within the cutoff."""
+    w = WORKLOADS[name]()
+    assert _walk_and_compare(make_gpu(w), w, 14) >= 3
+
+
+def test_dense_cells_past_the_list_estimate():
+    """A block at twice the mean density overflows the first list size (estimated from the
+    mean density): its cells are tested pair by pair, the lists grow at the next call, and
+    after the next rebuild they hold those cells too.  Pair sets stay exact throughout."""
+    w = configs.verlet(configs.cell_sorting(n=4000, side=20.0, seed=31), skin=0.3)
+    rng = np.random.default_rng(5)
+
+    def lattice(lo, hi, a):
+        g1 = np.arange(lo, hi, a, dtype=np.float32)
+        return np.stack(np.meshgrid(g1, g1, g1, indexing="ij"), axis=-1).reshape(-1, 3)
+
+    block = lattice(2.5, 14.0, 1.0)                     # 12^3 at spacing r0
+    sparse = lattice(0.8, 20.0, 20.0 / 12)
+    sparse = sparse[np.any((sparse < 1.5) | (sparse > 14.5), axis=1)]
+    x = np.concatenate([block, sparse])
+    x = x + rng.uniform(-0.05, 0.05, size=x.shape).astype(np.float32)
+    n = len(x)
+    w = dataclasses.replace(w, x=configs.in_box(x, w.dim[0]), type=w.type[:n], radius=w.radius[:n],
+                            imass=w.imass[:n])
+    w = dataclasses.replace(_relaxed(w, steps=30), dt=0.0005)   # several steps between rebuilds
+    g = make_gpu(w)
+
+    def force_rebuild(k):
+        if k == 4:   # re-setting a wall re-lays the arena out: every Verlet simulation rebuilds
+            g.set_boundary(0, abi.BOUNDARY_PERIODIC)
+
+    assert _walk_and_compare(g, w, 10, force_rebuild) >= 4

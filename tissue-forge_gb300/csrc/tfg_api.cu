@@ -476,6 +476,11 @@ TFG_API int tfg_batch_set_boundary_potential(tfg_engine *eng, int sim, int wall,
 TFG_API int tfg_batch_get_reductions(tfg_engine *eng, int sim, tfg_reductions *out) {
     return reductions_sim(eng, sim, out);
 }
+TFG_API int tfg_set_pair_lists(tfg_engine *eng, int enable) {
+    if (!eng) return TFG_E_INVAL;
+    eng->lists_wanted = enable != 0;   // applied at the next step; lists fill at the next rebuild
+    return TFG_OK;
+}
 TFG_API int tfg_get_verlet(tfg_engine *eng, int64_t *rebuilds, float *maxdx) {
     if (!eng) return TFG_E_INVAL;
     return verlet_sim(eng, 0, rebuilds, maxdx);

@@ -93,6 +93,7 @@ struct SimParams {
     // device fields are written by k_tick and k_advance; the host writes 2 to
     // verlet_rebuild to force a rebuild at the next step.
     float skin;              // min(h) - cutoff
+    float rlist2;            // (cutoff + skin)^2 with a relative margin: pair-list radius
     int32_t verlet_rebuild;  // device: this step re-bins and rebuilds the pair lists
     uint32_t verlet_maxdx2;  // device: max |x - oldx|^2 after the last advance (float bits)
     float verlet_maxdx;      // device: largest displacement at the last check (0 on a rebuild)

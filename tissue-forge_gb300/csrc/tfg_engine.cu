@@ -573,6 +573,9 @@ int add_sim(tfg_engine *eng, const tfg_engine_desc *d, int *out) {
     P.seed = d->seed;
     // engine_verlet_update (tfEngine.cpp:231): skin = min(h) - cutoff, in FP32
     P.skin = std::fmin(P.h[0], std::fmin(P.h[1], P.h[2])) - P.cutoff;
+    // a pair within the cutoff after both partners moved at most skin/2 was within
+    // cutoff + skin at the rebuild; the margin covers the FP32 rounding of r2
+    P.rlist2 = (P.cutoff + P.skin) * (P.cutoff + P.skin) * 1.0001f;
     P.verlet_rebuild = 2;
     S.maxc = std::max(P.cdim[0], std::max(P.cdim[1], P.cdim[2]));
     S.orig.assign((size_t)3 * S.maxc, 0.f);
@@ -684,6 +687,86 @@ int commit(tfg_engine *eng) {
         CK(cudaStreamSynchronize(eng->stream));
         if ((rc = check_launch(eng))) return rc;
     }
+    return prepare_lists(eng, relaid);
+}
+
+namespace {
+
+// Entries per home cell for the Verlet pair lists: twice the mean half-shell pair count
+// within the list radius of the densest simulation, plus room for the chunk markers.
+int estimate_list_k(const tfg_engine *eng) {
+    double best = 0.0;
+    for (int k : eng->order) {
+        const SimHost &S = eng->sims[k];
+        if (!(S.P.flags & TFG_ENGINE_VERLET) || S.n == 0) continue;
+        const double vol = (double)S.P.dim[0] * S.P.dim[1] * S.P.dim[2];
+        const double rl = (double)S.P.cutoff + S.P.skin;
+        const double per_cell = (double)S.n / S.P.ncells;
+        best = std::max(best, per_cell * (S.n / vol) * (2.0 / 3.0) * 3.14159265358979 * rl * rl * rl);
+    }
+    const int k = (int)std::ceil(2.0 * best) + 4 * 128;   // chunks start 128-entry groups
+    return (k + 127) & ~127;
+}
+
+int alloc_lists(tfg_engine *eng) {
+    const size_t cells = (size_t)std::max(eng->ncells, 1);
+    int rc;
+    if ((rc = ensure(eng, &eng->vlen, eng->vlen_cap, cells)) ||
+        (rc = ensure(eng, &eng->vlist, eng->vlist_cap, cells * (size_t)eng->list_k)))
+        return rc;
+    CK(cudaMemsetAsync(eng->vlen, 0xff, sizeof(int32_t) * cells, eng->stream));   // -1: no list
+    return TFG_OK;
+}
+
+}  // namespace
+
+int prepare_lists(tfg_engine *eng, bool relaid) {
+    bool any = false;
+    for (int k : eng->order) any |= (eng->sims[k].P.flags & TFG_ENGINE_VERLET) != 0;
+    const bool use = any && eng->lists_wanted && use_tile(eng) && !eng->has_dpd && !(eng->has_flux && eng->nspec > 0);
+    if (!use) {
+        if (eng->lists_on) eng->gen++;
+        eng->lists_on = false;
+        return TFG_OK;
+    }
+    if (!eng->list_need) {
+        int rc;
+        if ((rc = dalloc(eng, &eng->list_need, 1))) return rc;
+        CK(cudaMemsetAsync(eng->list_need, 0, sizeof(int), eng->stream));
+        CK(cudaMallocHost((void **)&eng->list_need_host, sizeof(int)));
+        *eng->list_need_host = 0;
+        CK(cudaEventCreateWithFlags(&eng->ev_need, cudaEventDisableTiming));
+    }
+    if (!eng->lists_on || relaid) {
+        eng->list_k = std::max(eng->list_k, estimate_list_k(eng));
+        int rc = alloc_lists(eng);
+        if (rc) return rc;
+        eng->lists_on = true;
+        eng->gen++;
+    }
+    if (eng->split != 1) {   // lists are kept per home cell
+        eng->split = 1;
+        eng->gen++;
+    }
+    return TFG_OK;
+}
+
+int check_lists(tfg_engine *eng) {
+    if (!eng->lists_on || !eng->need_pending) return TFG_OK;
+    const cudaError_t e = cudaEventQuery(eng->ev_need);
+    if (e == cudaErrorNotReady) {
+        cudaGetLastError();
+        return TFG_OK;
+    }
+    CK(e);
+    eng->need_pending = false;
+    const int need = *eng->list_need_host;
+    if (need <= eng->list_k) return TFG_OK;
+    // lists that did not fit are evaluated with candidate tests until the next rebuild
+    eng->list_k = ((int)(need * 1.25) + 127) & ~127;
+    int rc = alloc_lists(eng);
+    if (rc) return rc;
+    eng->gen++;
     return TFG_OK;
 }
 
@@ -723,6 +806,12 @@ PairKernelArgs pair_args(tfg_engine *eng) {
     a.has_dpd = eng->has_dpd;
     a.flux_sub = -1;
     a.has_flux = eng->has_flux;
+    if (eng->lists_on) {
+        a.vlist = eng->vlist;
+        a.vlen = eng->vlen;
+        a.list_k = eng->list_k;
+        a.list_need = eng->list_need;
+    }
     return a;
 }
 
@@ -843,8 +932,9 @@ int run_steps(tfg_engine *eng, int nsteps) {
     // After any change of the captured launch arguments one step runs eagerly (it also sets
     // every kernel's launch attributes up); the others replay the captured step of the
     // current buffer parity.  With phase timing on, every step writes its phase stamps.
+    int rc = check_lists(eng);
+    if (rc) return rc;
     for (int k = 0; k < nsteps; k++) {
-        int rc;
         if (eng->use_graphs && eng->eager_gen == eng->gen) {
             rc = graph_step(eng);
         } else {
@@ -852,6 +942,11 @@ int run_steps(tfg_engine *eng, int nsteps) {
             eng->eager_gen = eng->gen;
         }
         if (rc) return rc;
+    }
+    if (eng->lists_on && !eng->need_pending) {
+        CK(cudaMemcpyAsync(eng->list_need_host, eng->list_need, sizeof(int), cudaMemcpyDeviceToHost, eng->stream));
+        CK(cudaEventRecord(eng->ev_need, eng->stream));
+        eng->need_pending = true;
     }
     return TFG_OK;
 }
@@ -861,7 +956,7 @@ int run_steps(tfg_engine *eng, int nsteps) {
 // re-bin (idempotent on sorted data); the flux increments the trials add are saved and
 // restored, so the engine state is unchanged.
 int autotune(tfg_engine *eng) {
-    if (!use_tile(eng) || eng->n == 0) {
+    if (!use_tile(eng) || eng->n == 0 || eng->lists_on) {
         eng->split = 1;
         return TFG_OK;
     }
@@ -989,10 +1084,12 @@ void destroy(tfg_engine *eng) {
                     eng->slot_of_id, eng->scan_sums, eng->cell_sim, eng->overflow_list, eng->overflow_count,
                     eng->sims_dev, eng->corig, eng->pots, eng->blob, eng->fluxes, eng->rforce, eng->type_mass,
                     eng->type_dyn, eng->species_flags, eng->bonds, eng->bond_slot, eng->angles, eng->bpots,
-                    eng->bblob, eng->red, eng->err, eng->oldx};
+                    eng->bblob, eng->red, eng->err, eng->oldx, eng->vlist, eng->vlen, eng->list_need};
     for (void *p : bufs) cudaFree(p);
     for (int k = 0; k < 5; k++)
         if (eng->ev[k]) cudaEventDestroy(eng->ev[k]);
+    if (eng->ev_need) cudaEventDestroy(eng->ev_need);
+    if (eng->list_need_host) cudaFreeHost(eng->list_need_host);
     if (eng->own_stream && eng->stream) cudaStreamDestroy(eng->stream);
     delete eng;
 }

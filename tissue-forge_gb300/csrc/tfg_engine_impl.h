@@ -56,6 +56,17 @@ struct tfg_engine {
     float4 *force = nullptr;
     float4 *oldx = nullptr;          // Verlet reference positions by slot
     int oldx_cap = 0;
+    // Verlet pair lists of the tiled pass (table variants): list_k entries per home cell
+    bool lists_wanted = true;        // tfg_set_pair_lists
+    bool lists_on = false;
+    uint32_t *vlist = nullptr;
+    int32_t *vlen = nullptr;
+    size_t vlist_cap = 0, vlen_cap = 0;
+    int list_k = 0;
+    int *list_need = nullptr;        // device: largest list a build asked for
+    int *list_need_host = nullptr;   // pinned copy, read once its event has completed
+    cudaEvent_t ev_need = nullptr;
+    bool need_pending = false;
     int32_t *count = nullptr, *start = nullptr, *lidx = nullptr, *tmp_id = nullptr, *tmp_src = nullptr,
             *dest = nullptr, *slot_of_id = nullptr, *scan_sums = nullptr, *cell_sim = nullptr;
     int *overflow_list = nullptr, *overflow_count = nullptr;
@@ -147,6 +158,8 @@ int flux_substeps(tfg_engine *eng);  // one_step without the host clock
 int graph_step(tfg_engine *eng);                // one step replayed from a captured graph
 int run_steps(tfg_engine *eng, int nsteps);     // nsteps steps, graphs where they apply
 int autotune(tfg_engine *eng);
+int prepare_lists(tfg_engine *eng, bool relaid);  // allocate / invalidate the Verlet pair lists
+int check_lists(tfg_engine *eng);                 // grow them when a build asked for more
 PairKernelArgs pair_args(tfg_engine *eng);
 const TilePlan &tile_plan(tfg_engine *eng, int split);
 bool use_tile(const tfg_engine *eng);

@@ -73,7 +73,16 @@ struct PairKernelArgs {
                                 // nr_fluxsteps - 1 > flux_sub take part); -1: the full pass
     bool has_dpd;               // any type pair uses a DPD potential
     bool has_flux;              // any type pair has fluxes
+    // Verlet pair lists (tiled pass, table potentials): per home cell, the staged-index
+    // pairs (i | k << 16) within the list radius found at the simulation's last rebuild,
+    // one kListEnd marker after each staging chunk, in interleaved groups of 128
+    uint32_t *vlist;            // list_k entries per home cell (a multiple of 128)
+    int32_t *vlen;              // entries of each home cell's list; -1: none (candidate tests)
+    int list_k;
+    int *list_need;             // largest list a build asked for (atomicMax)
 };
+
+constexpr uint32_t kListEnd = 0xffffffffu;
 
 // Full-stencil kernel: one thread per particle, no atomics.  General path (any number
 // of species); force[] must hold the initial force (external + random, density W(0)).

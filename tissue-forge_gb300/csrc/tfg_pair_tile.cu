@@ -59,6 +59,12 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
+// Pair lists are stored in groups of 128 entries, interleaved so that one 16-byte load per
+// lane fetches four batches of 32: sequential entry p of a list sits at list_slot(p), and
+// component c of lane L's load is entry 32 c + L of the group.  Each staged chunk's
+// entries end with a kListEnd marker and the next chunk starts at the next group.
+__device__ __forceinline__ int list_slot(int p) { return (p & ~127) | ((p & 31) << 2) | ((p >> 5) & 3); }
+
 struct TileArgs {
     PairKernelArgs a;
     int *overflow_list;    // home cells handed to the overflow kernel
@@ -333,7 +339,11 @@ __device__ __forceinline__ void flush(const PairKernelArgs &a, ST &S, int b0, in
     else flush_call<kFlux, kSig>(a, S, b0, b1, lane);
 }
 
-template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
+// kVerlet (table variants): simulations in Verlet mode record, on their rebuild steps, the
+// pairs within the list radius of every staged chunk, and on the other steps evaluate
+// those lists instead of testing every candidate pair (engine_flag_verlet; the reference
+// keeps its sorted windows between rebuilds instead, tf_runner_dopair.cpp:115-117).
+template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false>
 __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
     using Staged = typename TileOf<kDPD, kFlux>::S;
     constexpr int kCap = Staged::cap;
@@ -379,6 +389,17 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
             cur_rb = P.red_base;
         }
         const float cutoff2 = P.cutoff2;
+        // pair list of this item: 1 = build it (candidate tests record the pairs within the
+        // list radius), 2 = walk it, 0 = candidate tests only
+        int lmode = 0, lcount = 0, lvalid = 0;
+        uint32_t *lst = nullptr;
+        float rlist2 = 0.f;
+        if (kVerlet && (P.flags & TFG_ENGINE_VERLET)) {
+            lvalid = a.vlen[item];
+            lmode = P.verlet_rebuild ? 1 : (lvalid >= 0 ? 2 : 0);
+            lst = a.vlist + (size_t)item * a.list_k;
+            rlist2 = P.rlist2;
+        }
         const int t0 = 13 + grp * per, t1 = t0 + per;
         int li, lj, lk;
         cell_loc(P, home, li, lj, lk);
@@ -408,6 +429,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                 const int k = atomicAdd(T.overflow_count, 1);
                 T.overflow_list[k] = home;
             }
+            if (kVerlet && lmode == 1 && lane == 0) a.vlen[item] = -1;
             continue;
         }
         stage<kDPD, kFlux, kSig>(a, S, 0, h0, nh, 13, lane);
@@ -434,6 +456,10 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
         int t = t0 < 14 ? 14 : t0;     // next neighbour task to stage
         bool with_self = (t0 == 13);
         while (with_self || t < t1) {
+            // walk: the chunk's first group of list entries loads while its segments are staged
+            uint4 gnext = make_uint4(kListEnd, kListEnd, kListEnd, kListEnd);
+            if (kVerlet && lmode == 2 && lcount + 4 * lane < lvalid)
+                gnext = *reinterpret_cast<const uint4 *>(lst + lcount + 4 * lane);
             // stage as many neighbour segments as fit after the home cell
             int end = nh;
             while (t < t1) {
@@ -449,7 +475,58 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
             const int ntgt = end - tbeg;
             with_self = false;
             int qhead = 0, qtail = 0;
-            if (ntgt > 0) {
+            if (kVerlet && lmode == 2) {
+                // the list entries of this chunk, up to its marker: re-test each pair at the
+                // cutoff with the current positions, queue the hits, evaluate 32 at a time
+                bool done = false;
+                int c = 0;              // batch of 32 within the current group
+                uint4 gcur = gnext;
+                for (;;) {
+                    if (!done) {
+                        if (c == 0) {   // the next group loads while this one is tested
+                            const bool end_here =
+                                __any_sync(0xffffffffu, gcur.x == kListEnd || gcur.y == kListEnd ||
+                                                            gcur.z == kListEnd || gcur.w == kListEnd);
+                            gnext = make_uint4(kListEnd, kListEnd, kListEnd, kListEnd);
+                            if (!end_here && lcount + 128 + 4 * lane < lvalid)
+                                gnext = *reinterpret_cast<const uint4 *>(lst + lcount + 128 + 4 * lane);
+                        }
+                        const uint32_t e = c == 0 ? gcur.x : (c == 1 ? gcur.y : (c == 2 ? gcur.z : gcur.w));
+                        const uint32_t mm = __ballot_sync(0xffffffffu, e == kListEnd);
+                        const int fm = mm ? __ffs(mm) - 1 : 32;
+                        const int I = e & 0xffff, K = e >> 16;
+                        bool hit = false;
+                        if (lane < fm && I < end && K < end) {
+                            const float4 pi4 = S.pos[I], pk = S.pos[K], s4 = S.sh4[K];
+                            float3 dx;
+                            const float r2 = pair_r2(make_float3(pi4.x, pi4.y, pi4.z), make_float3(s4.x, s4.y, s4.z),
+                                                     make_float3(pk.x, pk.y, pk.z), dx);
+                            hit = r2 <= cutoff2;
+                        }
+                        const uint32_t m = __ballot_sync(0xffffffffu, hit);
+                        if (hit) S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = e;
+                        qtail += __popc(m);
+                        done = fm < 32;
+                        if (++c == 4 || done) {
+                            c = 0;
+                            lcount += 128;
+                            gcur = gnext;
+                        }
+                        __syncwarp();
+                    }
+                    const int avail = qtail - qhead;
+                    if (avail >= 32 || (done && avail > 0)) {
+                        const int take = avail < 32 ? avail : 32;
+                        const bool act = lane < take;
+                        const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
+                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, lane, epot, vir);
+                        qhead += take;
+                        __syncwarp();
+                    } else if (done) {
+                        break;
+                    }
+                }
+            } else if (ntgt > 0) {
                 if constexpr (kDPD || kFlux) {
                     // The DPD and flux evaluations are long: the candidate walk over (block of 32
                     // targets, i) pauses whenever 32 hits are queued, so the evaluation has a
@@ -512,6 +589,15 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                             float3 dx;
                             const float r2 = pair_r2(make_float3(pi4.x, pi4.y, pi4.z), shk, xk, dx);
                             const bool hit = i < ilim && r2 <= cutoff2;
+                            if (kVerlet && lmode == 1) {
+                                const bool lh = i < ilim && r2 <= rlist2;
+                                const uint32_t lm = __ballot_sync(0xffffffffu, lh);
+                                if (lh) {
+                                    const int lp = lcount + __popc(lm & lanemask_lt());
+                                    if (lp < a.list_k) lst[list_slot(lp)] = (uint32_t)i | ((uint32_t)k << 16);
+                                }
+                                lcount += __popc(lm);
+                            }
                             const uint32_t m = __ballot_sync(0xffffffffu, hit);
                             if (hit)
                                 S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)k << 16);
@@ -533,10 +619,18 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                 }
                 __syncwarp();
             }
+            if (kVerlet && lmode == 1) {   // end of this chunk's entries; the next starts a group
+                if (lane == 0 && lcount < a.list_k) lst[list_slot(lcount)] = kListEnd;
+                lcount = (lcount + 128) & ~127;
+            }
             flush<kDPD, kFlux, kSig>(a, S, nh, end, lane);
             __syncwarp();
         }
         flush<kDPD, kFlux, kSig>(a, S, 0, nh, lane);
+        if (kVerlet && lmode == 1 && lane == 0) {
+            a.vlen[item] = lcount <= a.list_k ? lcount : -1;
+            atomicMax(a.list_need, lcount);
+        }
         __syncwarp();
     }
     if (lane == 0) base = atomicAdd(T.overflow_count + 1, kGrab);
@@ -679,7 +773,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
     }
 }
 
-template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
+template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false>
 void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
     const size_t base = sizeof(typename TileOf<kDPD, kFlux>::S) * kWarps;
     const size_t smem_max = base + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxSmemPots;
@@ -688,19 +782,19 @@ void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
     static size_t occ_smem = 0;
     static int per_sm = 1;
     if (!configured) {
-        cudaFuncSetAttribute(k_pair_tile<kDPD, kFlux, kDensity, kSig>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem_max);
+        cudaFuncSetAttribute(k_pair_tile<kDPD, kFlux, kDensity, kSig, kVerlet>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
         configured = true;
     }
     if (occ_smem != smem) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_tile<kDPD, kFlux, kDensity, kSig>, kWarps * 32,
-                                                      smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_tile<kDPD, kFlux, kDensity, kSig, kVerlet>,
+                                                      kWarps * 32, smem);
         if (per_sm < 1) per_sm = 1;
         occ_smem = smem;
     }
     const int want = (T.a.ncells * T.split + kWarps - 1) / kWarps;
     const int grid = std::max(1, std::min(want, sms * per_sm));
-    k_pair_tile<kDPD, kFlux, kDensity, kSig><<<grid, kWarps * 32, smem, s>>>(T);
+    k_pair_tile<kDPD, kFlux, kDensity, kSig, kVerlet><<<grid, kWarps * 32, smem, s>>>(T);
     k_pair_overflow<kDPD, kFlux, kDensity, kSig><<<sms, 256, 0, s>>>(T);
 }
 
@@ -749,7 +843,13 @@ void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overfl
     const bool dpd = a.has_dpd, flux = a.nspec > 0 && a.has_flux;
     const bool dens = !(a.flags & TFG_ENGINE_NO_DENSITY);
     if (signature) {
-        launch_variant<false, false, false, true>(T, s, sms);
+        if (a.vlist) launch_variant<false, false, false, true, true>(T, s, sms);
+        else launch_variant<false, false, false, true>(T, s, sms);
+        return;
+    }
+    if (a.vlist && !dpd && !flux) {   // Verlet pair lists (some simulation in Verlet mode)
+        if (dens) launch_variant<false, false, true, false, true>(T, s, sms);
+        else launch_variant<false, false, false, false, true>(T, s, sms);
         return;
     }
 #define TFG_PAIR_DISPATCH(D, F)                                          \

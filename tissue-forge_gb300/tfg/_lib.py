@@ -57,6 +57,7 @@ def lib():
     L.tfg_download.argtypes = [E, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P]
     L.tfg_get_reductions.argtypes = [E, C.POINTER(abi.Reductions)]
     L.tfg_get_verlet.argtypes = [E, C.POINTER(C.c_int64), C.POINTER(C.c_float)]
+    L.tfg_set_pair_lists.argtypes = [E, C.c_int]
     L.tfg_get_phase_ms.argtypes = [E, C.POINTER(C.c_float)]
     L.tfg_set_phase_timing.argtypes = [E, C.c_int]
     L.tfg_probe_fp32_tflops.argtypes = [C.c_int, C.POINTER(C.c_double)]

@@ -237,3 +237,28 @@ def verlet(w, skin=0.2):
     cells = tuple(max(3, int(math.floor(d / (w.cutoff * (1.0 + skin))))) for d in w.dim)
     return dataclasses.replace(w, cells=cells, flags=w.flags | abi.ENGINE_VERLET,
                                name=w.name + "_verlet")
+
+
+def lj_fluid(n=2_000_000, density=0.85, cutoff=2.5, temperature=0.5, steps=500, seed=5):
+    """Lennard-Jones fluid (the bonded fluid's 12-6 potential, no bonds) started without
+    overlaps: a simple cubic lattice at the given density, jittered, with Maxwell
+    velocities.  Stable without the reference's displacement clamp, so it also runs in
+    Verlet mode."""
+    rng = np.random.default_rng(np.random.PCG64(5000 + seed))
+    m = int(round((n) ** (1.0 / 3.0)))
+    n = m ** 3
+    side = float((n / density) ** (1.0 / 3.0))
+    a = side / m
+    g = (np.arange(m) + 0.5) * a
+    x = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(n, 3)
+    x = in_box(x + rng.uniform(-0.05 * a, 0.05 * a, size=x.shape), side)
+    v = rng.normal(0.0, math.sqrt(temperature), size=(n, 3))
+    v -= v.mean(axis=0)
+    c = cells_for(side, cutoff)
+    w = Workload(
+        name="lj_fluid", origin=(0.0, 0.0, 0.0), dim=(side,) * 3, cells=(c, c, c), cutoff=cutoff,
+        dt=0.002, steps=steps, x=x, type=np.zeros(n, np.int32), v=v.astype(np.float32),
+        radius=np.ones(n, np.float32), imass=np.ones(n, np.float32), max_type=1,
+        dynamics=[abi.NEWTONIAN], mass=[1.0], seed=5000 + seed)
+    w.pots[(0, 0)] = PotSpec("lj", dict(min=0.1, max=cutoff, A=1.0, B=1.0, tol=0.0))
+    return w

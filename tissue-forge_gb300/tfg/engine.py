@@ -181,6 +181,9 @@ class Engine:
         self._chk(self.L.tfg_get_reductions(self.h, C.byref(r)), "get_reductions")
         return r
 
+    def set_pair_lists(self, enable):
+        self._chk(self.L.tfg_set_pair_lists(self.h, 1 if enable else 0), "set_pair_lists")
+
     def verlet(self):
         """(rebuilds so far, largest displacement since the last rebuild) in Verlet mode."""
         nb, m = C.c_int64(), C.c_float()
