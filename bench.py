@@ -56,6 +56,11 @@ WORKLOADS = {
                               "at density 0.85, cutoff 2.5, dt 0.002", bytes_per_particle=80),
     "cell_sorting": dict(desc="cell sorting: 4,000 particles, box 20, cutoff 3, shifted Morse, overdamped",
                          bytes_per_particle=48),
+    "lj_fluid": dict(desc="LJ 12-6 fluid from a jittered lattice: 2,000,376 particles at density 0.85, cutoff 2.5, "
+                          "T 0.5, dt 0.002, cell lists (cell edge >= cutoff)", bytes_per_particle=64),
+    "lj_fluid_verlet": dict(desc="the lj_fluid workload in Verlet mode (engine_flag_verlet): cell edge >= 1.2 cutoff, "
+                                 "re-binning only when 2 maxdx > skin, device pair lists between rebuilds",
+                            bytes_per_particle=64),
 }
 
 # Algorithmic flops per interacting pair (one evaluation serving both particles) and per
@@ -81,7 +86,32 @@ def make_workload(name, seed, n=None, relax=None):
         if n:
             return configs.cell_sorting(n=n, side=20.0 * (n / 4000) ** (1.0 / 3.0), seed=seed)
         return configs.cell_sorting(seed=seed)
+    if name == "lj_fluid":
+        return configs.lj_fluid(n=n or 2_000_000, seed=5 + seed)
+    if name == "lj_fluid_verlet":
+        return configs.verlet(configs.lj_fluid(n=n or 2_000_000, seed=5 + seed), skin=VERLET_SKIN)
     raise SystemExit("unknown workload " + name)
+
+
+VERLET_SKIN = 0.2   # cell edge >= (1 + VERLET_SKIN) * cutoff for the Verlet workload
+
+
+def timed_rate(eng, n, steps, warmup, flush, stream, world=1):
+    """particle-steps/s of `steps` single steps, L2 flushed before each (CUDA events)."""
+    import torch
+    for _ in range(warmup):
+        eng.step(1, sync=False)
+    eng.set_phase_timing(False)
+    eng.step(2)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        eng.step(1, sync=False)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    return world * n * steps / (sum(a.elapsed_time(b) for a, b in ev) * 1e-3)
 
 
 def pair_flops(w):
@@ -517,6 +547,7 @@ def run_single(args, rank, world, dev, dist):
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
+    rebuilds0 = eng.verlet()[0] if w.flags & 4 else 0
     with ClockSampler(dev, clock_path("clocks_bench.csv")) as clk:
         for k in range(args.steps):
             flush.zero_()
@@ -524,6 +555,7 @@ def run_single(args, rank, world, dev, dist):
             eng.step(1, sync=False)
             ev[k][1].record(stream)
         torch.cuda.synchronize()
+    rebuilds1 = eng.verlet()[0] if w.flags & 4 else 0
     # phase split from stamped steps after the timed region (L2 flushed before each)
     eng.set_phase_timing(True)
     eng.step(2)
@@ -581,6 +613,23 @@ def run_single(args, rank, world, dev, dist):
             "kernel_ms": pair_ms_avg, "traffic": None,
             "step_hbm": {"achieved_gbs": bytes_alg / (step_ms * 1e-3) / 1e9, "peak_gbs": hbm, "peak_source": hbm_src,
                          "frac": bytes_alg / (step_ms * 1e-3) / 1e9 / hbm, "bytes_per_step": bytes_alg}}
+    verlet = None
+    if w.flags & 4:   # Verlet mode: the same fluid with cell lists, and Verlet without pair lists
+        rb_timed = rebuilds1 - rebuilds0
+        wc = make_workload("lj_fluid", rank, args.n or None)
+        cmp = {}
+        for label, ww, lists in (("cell_lists", wc, True), ("verlet_without_pair_lists", w, False)):
+            e = Engine(ww.desc(device=dev))
+            k = setup_model(e, ww)
+            e.set_stream(stream.cuda_stream)
+            e.set_pair_lists(lists)
+            cmp[label] = timed_rate(e, ww.n, args.steps, args.warmup, flush, stream, world)
+            del e, k
+        verlet = {"skin": float(min(d / c for d, c in zip(w.dim, w.cells)) - w.cutoff),
+                  "rebuilds_in_timed_steps": rb_timed, "steps": args.steps,
+                  "cell_lists_value": cmp["cell_lists"], "verlet_without_pair_lists_value": cmp["verlet_without_pair_lists"],
+                  "speedup_over_cell_lists": value / cmp["cell_lists"],
+                  "how": "same fluid, same steps and L2 flush; cell lists at cell edge >= cutoff"}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -601,6 +650,8 @@ def run_single(args, rank, world, dev, dist):
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
             "gpu_launches": launches_per_step(w.bonds is not None, w.angles is not None) * args.steps,
         }
+        if verlet:
+            line["verlet"] = verlet
         print(json.dumps(line), flush=True)
     del keep, keep2
 
