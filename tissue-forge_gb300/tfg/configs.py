@@ -33,8 +33,9 @@ from . import abi
 
 @dataclass
 class PotSpec:
-    """Arguments of one reference Potential factory call."""
-    kind: str                  # "morse" | "lj" | "harmonic" | "harmonic_angle" | "dpd"
+    """Arguments of one reference Potential factory call, or ("table") a potential as the
+    reference stores it: kind, flags, alpha, r0_plusone, a, b, n, c (tuples) and dpd."""
+    kind: str                  # "morse" | "lj" | "harmonic" | "harmonic_angle" | "dpd" | "table"
     args: dict
 
 
@@ -70,6 +71,15 @@ class Workload:
     nr_fluxsteps: int = 1
     boundaries: list = field(default_factory=list)  # (wall, kind, velocity, restore, radius)
     wall_pots: list = field(default_factory=list)   # (wall or -1, type, PotSpec)
+    # bonded potentials by slot, with each bond's and angle's slot (default: bond_pot in
+    # slot 0 for every bond, angle_pot in slot 1 for every angle)
+    bonded_pots: list = field(default_factory=list)
+    bond_slot: Optional[np.ndarray] = None
+    angle_slot: Optional[np.ndarray] = None
+    type_forces: list = field(default_factory=list)  # (type, mean, std, duration_steps)
+    flags_particles: Optional[np.ndarray] = None      # per-particle flags (frozen axes)
+    force_i: Optional[np.ndarray] = None              # (n,3) external force per particle
+    max_dist_fraction: float = 0.05                  # particle_max_dist_fraction
 
     @property
     def n(self):
@@ -80,6 +90,7 @@ class Workload:
         na = 0 if self.angles is None else len(self.angles)
         return abi.engine_desc(self.origin, self.dim, self.cells, self.cutoff, self.dt,
                                max_type=self.max_type, nr_species=self.nr_species,
+                               particle_max_dist_fraction=self.max_dist_fraction,
                                seed=self.seed, capacity=capacity or self.n,
                                max_bonds=nb, max_angles=na, device=device, flags=self.flags,
                                nr_fluxsteps=self.nr_fluxsteps)

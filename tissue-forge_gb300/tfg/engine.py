@@ -351,7 +351,7 @@ class Sim:
 def _potential(spec, cache):
     if cache is None:
         return Potential.from_spec(spec)
-    key = (spec.kind, tuple(sorted(spec.args.items())))
+    key = (spec.kind, tuple(sorted((k, tuple(v) if isinstance(v, list) else v) for k, v in spec.args.items())))
     p = cache.get(key)
     if p is None:
         p = cache[key] = Potential.from_spec(spec)
@@ -376,6 +376,8 @@ def setup_model(eng, w, keep=None, pot_cache=None):
         mean, std, dur = w.random_force
         for t in range(w.max_type):
             eng.set_random_force(t, mean, std, dur)
+    for (t, mean, std, dur) in w.type_forces:
+        eng.set_random_force(t, mean, std, dur)
     for (wall, kind, vel, restore, radius) in w.boundaries:
         eng.set_boundary(wall, kind, vel, restore, radius)
     for (wall, t, spec) in w.wall_pots:
@@ -390,11 +392,18 @@ def setup_model(eng, w, keep=None, pot_cache=None):
         p = _potential(w.angle_pot, pot_cache)
         pots.append(p)
         eng.set_bonded_potential(1, p.ptr)
-    eng.load(w.x, v=w.v, type=w.type, radius=w.radius, imass=w.imass, species=w.species)
+    for slot, spec in enumerate(w.bonded_pots):
+        p = _potential(spec, pot_cache)
+        pots.append(p)
+        eng.set_bonded_potential(slot, p.ptr)
+    eng.load(w.x, v=w.v, type=w.type, radius=w.radius, imass=w.imass, flags=w.flags_particles, species=w.species,
+             force_i=w.force_i)
     if w.bonds is not None:
-        eng.load_bonds(w.bonds[:, 0], w.bonds[:, 1], np.zeros(len(w.bonds), np.int32))
+        bs = w.bond_slot if w.bond_slot is not None else np.zeros(len(w.bonds), np.int32)
+        eng.load_bonds(w.bonds[:, 0], w.bonds[:, 1], bs)
     if w.angles is not None:
-        eng.load_angles(w.angles[:, 0], w.angles[:, 1], w.angles[:, 2], np.ones(len(w.angles), np.int32))
+        aslot = w.angle_slot if w.angle_slot is not None else np.ones(len(w.angles), np.int32)
+        eng.load_angles(w.angles[:, 0], w.angles[:, 1], w.angles[:, 2], aslot)
     if keep is not None:
         keep.extend(pots)
     return pots

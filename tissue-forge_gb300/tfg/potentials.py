@@ -62,8 +62,17 @@ class Potential:
         return cls._make(lib().tfg_potential_dpd, alpha, gamma, sigma, cutoff, 1 if shifted else 0, kind="dpd")
 
     @classmethod
+    def from_table(cls, kind, flags, alpha, r0_plusone, a, b, n, c, dpd=(0.0, 0.0, 0.0)):
+        """A potential given as the reference stores it (struct Potential, tfPotential.h:213-253):
+        the table is used as is, not rebuilt.  kind 1 is DPD (c unused)."""
+        return RawPotential(kind, flags, alpha, r0_plusone, a, b, n, c, dpd)
+
+    @classmethod
     def from_spec(cls, spec):
         a = spec.args
+        if spec.kind == "table":
+            return cls.from_table(a["kind"], a["flags"], a["alpha"], a["r0_plusone"], a["a"], a["b"], a["n"], a["c"],
+                                  a.get("dpd", (0.0, 0.0, 0.0)))
         if spec.kind == "morse":
             return cls.morse(a["d"], a["a"], a["r0"], a["min"], a["max"], a["tol"], a["shifted"])
         if spec.kind == "lj":
@@ -75,3 +84,28 @@ class Potential:
         if spec.kind == "dpd":
             return cls.dpd(a["alpha"], a["gamma"], a["sigma"], a["cutoff"], a["shifted"])
         raise ValueError(spec.kind)
+
+
+class RawPotential(Potential):
+    """A potential whose descriptor and table live in Python memory (for tables read from a
+    file).  set_potential copies both, so this object only needs to outlive that call."""
+
+    def __init__(self, kind, flags, alpha, r0_plusone, a, b, n, c, dpd):
+        import numpy as np
+        self._c = np.ascontiguousarray(c, np.float32) if c is not None and len(c) else None
+        st = abi.Potential()
+        st.kind = int(kind)
+        st.flags = int(flags)
+        for k in range(4):
+            st.alpha[k] = float(alpha[k]) if k < len(alpha) else 0.0
+        st.r0_plusone = float(r0_plusone)
+        st.a = float(a)
+        st.b = float(b)
+        st.n = int(n)
+        st.c = self._c.ctypes.data_as(C.POINTER(C.c_float)) if self._c is not None else None
+        st.dpd_alpha, st.dpd_gamma, st.dpd_sigma = (float(v) for v in dpd)
+        self._st = st
+        super().__init__(C.pointer(st), "table" if int(kind) != abi.POTENTIAL_KIND_DPD else "dpd")
+
+    def __del__(self):
+        self.ptr = None
