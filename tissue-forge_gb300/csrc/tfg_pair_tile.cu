@@ -86,6 +86,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
     const float3 sh = make_float3(s4.x, s4.y, s4.z);
     float3 dx;
     const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z), sh, make_float3(pk.x, pk.y, pk.z), dx);
+    if (r2 > P.cutoff2) return;   // a candidate that only the table loop's looser filter passed
     const float r = __fsqrt_rn(r2);
     const bool flux_only = kFlux && a.flux_sub >= 0;
     if (kDensity && !flux_only) {
@@ -169,6 +170,12 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P
     const int I = e & 0xffff, K = e >> 16;
     if (kSig) {
         if (active) {
+            // the pair decision proper (the table loop queues candidates with a looser filter)
+            const float4 pi = S.pos[I], pk = S.pos[K], s4 = S.sh4[K];
+            float3 dx;
+            if (pair_r2(make_float3(pi.x, pi.y, pi.z), make_float3(s4.x, s4.y, s4.z), make_float3(pk.x, pk.y, pk.z),
+                        dx) > P.cutoff2)
+                return;
             atomicAdd(reinterpret_cast<int *>(&S.acc[I].x), 1);
             atomicAdd(reinterpret_cast<int *>(&S.acc[K].x), 1);
             const uint32_t idi = (uint32_t)__float_as_int(T.a.aux[S.gslot[I]].w);
@@ -574,6 +581,10 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                 } else {
                     // each lane keeps one target k in registers; the home particles i are
                     // broadcast to all lanes.  Self targets (k < nh) pair only with i < k.
+                    // Candidates are queued by a cheaper test, x_i - (x_k + shift) with FMA
+                    // against the squared cutoff plus 1e-5 relative (far above the few-ulp
+                    // difference to the reference's (x_i - shift) - x_k); the evaluation and
+                    // the signature then apply the reference's test, so the pair set is exact.
                     for (int kb = tbeg; kb < end; kb += 32) {
                         const int k = kb + lane;
                         float4 pk = make_float4(0.f, 0.f, 0.f, 0.f), s4 = pk;
@@ -583,12 +594,13 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                         }
                         const int ilim = k < end ? (k < nh ? k : nh) : 0;
                         const int iend = kb + 31 < nh ? kb + 31 : nh;
-                        const float3 xk = make_float3(pk.x, pk.y, pk.z), shk = make_float3(s4.x, s4.y, s4.z);
+                        const float xs = pk.x + s4.x, ys = pk.y + s4.y, zs = pk.z + s4.z;
+                        const float cut_f = cutoff2 * 1.00001f;
                         for (int i = 0; i < iend; i++) {
                             const float4 pi4 = S.pos[i];
-                            float3 dx;
-                            const float r2 = pair_r2(make_float3(pi4.x, pi4.y, pi4.z), shk, xk, dx);
-                            const bool hit = i < ilim && r2 <= cutoff2;
+                            const float ddx = pi4.x - xs, ddy = pi4.y - ys, ddz = pi4.z - zs;
+                            const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
+                            const bool hit = i < ilim && r2 <= cut_f;
                             if (kVerlet && lmode == 1) {
                                 const bool lh = i < ilim && r2 <= rlist2;
                                 const uint32_t lm = __ballot_sync(0xffffffffu, lh);
