@@ -187,3 +187,25 @@ def test_dense_cells_past_the_list_estimate():
             g.set_boundary(0, abi.BOUNDARY_PERIODIC)
 
     assert _walk_and_compare(g, w, 10, force_rebuild) >= 4
+
+
+def test_full_size_list_walk_equals_candidate_tests():
+    """2.0M-particle LJ fluid in Verlet mode: at every step that does not rebuild, the pair
+    set walked through the lists equals the one the candidate tests find (signature of every
+    particle), and the engine's trajectory with lists stays with the one without."""
+    w = configs.verlet(configs.lj_fluid(n=2_000_000), skin=0.2)
+    g = make_gpu(w)
+    h = make_gpu(w)
+    h.set_pair_lists(False)
+    for _ in range(3):
+        g.step(4)
+        h.step(4)
+    rb = g.verlet()[0]
+    assert rb == h.verlet()[0]
+    gc, gh = g.pair_signature()        # walks the lists (no rebuild is pending: 2 maxdx < skin)
+    g.set_pair_lists(False)
+    cc, ch = g.pair_signature()        # candidate tests on the same state
+    assert np.array_equal(gc, cc) and np.array_equal(gh, ch)
+    assert int(gc.sum()) // 2 > 50_000_000
+    dev = _dev(g.download()["x"], h.download()["x"], w.dim)
+    assert dev.max() < 1e-3

@@ -708,6 +708,16 @@ int estimate_list_k(const tfg_engine *eng) {
     return (k + 127) & ~127;
 }
 
+// Pair lists take at most this many bytes; cells whose list does not fit under it keep
+// testing candidate pairs.
+constexpr size_t kMaxListBytes = size_t(16) << 30;
+
+int capped_list_k(const tfg_engine *eng, int k) {
+    const size_t cells = (size_t)std::max(eng->ncells, 1);
+    const size_t most = kMaxListBytes / sizeof(uint32_t) / cells;
+    return (int)std::min<size_t>((size_t)k, std::max<size_t>(most & ~size_t(127), 128));
+}
+
 int alloc_lists(tfg_engine *eng) {
     const size_t cells = (size_t)std::max(eng->ncells, 1);
     int rc;
@@ -738,7 +748,7 @@ int prepare_lists(tfg_engine *eng, bool relaid) {
         CK(cudaEventCreateWithFlags(&eng->ev_need, cudaEventDisableTiming));
     }
     if (!eng->lists_on || relaid) {
-        eng->list_k = std::max(eng->list_k, estimate_list_k(eng));
+        eng->list_k = capped_list_k(eng, std::max(eng->list_k, estimate_list_k(eng)));
         int rc = alloc_lists(eng);
         if (rc) return rc;
         eng->lists_on = true;
@@ -761,9 +771,10 @@ int check_lists(tfg_engine *eng) {
     CK(e);
     eng->need_pending = false;
     const int need = *eng->list_need_host;
-    if (need <= eng->list_k) return TFG_OK;
+    const int grown = capped_list_k(eng, ((int)(need * 1.25) + 127) & ~127);
+    if (need <= eng->list_k || grown <= eng->list_k) return TFG_OK;
     // lists that did not fit are evaluated with candidate tests until the next rebuild
-    eng->list_k = ((int)(need * 1.25) + 127) & ~127;
+    eng->list_k = grown;
     int rc = alloc_lists(eng);
     if (rc) return rc;
     eng->gen++;
