@@ -315,7 +315,7 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def serve_sample(args, dev, count, rate=200.0):
+def serve_sample(args, dev, count, rate=200.0, policy="sjf"):
     """A bounded sample of the served stream: the first `count` requests of the Poisson
     stream at `rate` requests/s, with their particles generated before the clock starts
     (client-side data)."""
@@ -328,10 +328,10 @@ def serve_sample(args, dev, count, rate=200.0):
     for r in reqs:
         r.t_arrival -= t_first
     srv = Server(budget_bytes=150 << 30, max_particles=args.serve_particles, quantum=args.quantum, device=dev,
-                 keep_results=False)
+                 keep_results=False, policy=policy)
     done = srv.run(reqs)
     s = summarize(done)
-    s.update({"max_concurrent": srv.max_concurrent, "chunks": srv.chunks, "quantum": args.quantum,
+    s.update({"policy": policy, "max_concurrent": srv.max_concurrent, "chunks": srv.chunks, "quantum": args.quantum,
               "max_particles_in_flight": args.serve_particles, "budget_bytes": 150 << 30,
               "rate_per_s": rate,
               "sample": "first %d of the 10,000 requests (arrivals re-based to t=0)" % count})
@@ -485,6 +485,10 @@ def run_ensemble(args, rank, world, dev, dist):
         work = serving["particle_steps"] / serving["requests"]
         rate = 0.5 * serving["achieved_particle_steps_per_s"] / work
         serving["at_sustainable_rate"] = serve_sample(args, dev, args.sustained_requests, rate=rate)
+    if serving is not None and args.fifo_compare:
+        f = serve_sample(args, dev, args.requests, policy="fifo")
+        serving["fifo_same_stream"] = {k: f[k] for k in ("p50_latency_s", "p99_latency_s", "mean_latency_s",
+                                                         "achieved_particle_steps_per_s", "max_concurrent")}
     if rank == 0:
         line = {
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
@@ -673,7 +677,9 @@ def main():
     ap.add_argument("--sims", type=int, default=256, help="simulations in the ensemble")
     ap.add_argument("--plain-steps", type=int, default=20, help="timed steps per simulation on the plain path")
     ap.add_argument("--requests", type=int, default=100, help="served-stream sample size (0: skip)")
-    ap.add_argument("--serve-particles", type=int, default=4_000_000, help="particles in flight cap")
+    ap.add_argument("--fifo-compare", type=int, default=1,
+                    help="also serve the sample first-come-first-served, for comparison (0: skip)")
+    ap.add_argument("--serve-particles", type=int, default=2_000_000, help="particles in flight cap")
     ap.add_argument("--quantum", type=int, default=50, help="largest chunk of steps between admissions")
     ap.add_argument("--seed", type=int, default=4)
     args = ap.parse_args()

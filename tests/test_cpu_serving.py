@@ -1,6 +1,6 @@
-"""Host logic of the request loop with a stand-in batch (no GPU): first-come-first-served
-admission under the particle cap and the byte budget, chunks cut at the earliest finishing
-simulation, every request run for exactly its step count."""
+"""Host logic of the request loop with a stand-in batch (no GPU): least-work-first and
+first-come-first-served admission under the particle cap and the byte budget, chunks cut at
+the earliest finishing simulation, every request run for exactly its step count."""
 import pytest
 
 from tfg import configs
@@ -95,7 +95,8 @@ def test_every_request_runs_exactly_its_steps():
 def test_fifo_admission_and_budget():
     reqs = _reqs()
     budget = 2 * max(footprint(r.workload) for r in reqs)
-    srv = Server(max_particles=10 ** 9, budget_bytes=budget, quantum=8, lane_factory=lambda mt, ns: FakeLane(mt, ns))
+    srv = Server(max_particles=10 ** 9, budget_bytes=budget, quantum=8, lane_factory=lambda mt, ns: FakeLane(mt, ns),
+                 policy="fifo")
     done = srv.run(reqs)
     admits = sorted(done, key=lambda r: (r.t_admit, r.rid))
     assert [r.rid for r in admits] == sorted(r.rid for r in done)   # first come, first served
@@ -103,3 +104,20 @@ def test_fifo_admission_and_budget():
     big = Request(99, 0.0, configs.cell_sorting(n=500_000, side=100.0, seed=1), 1)
     with pytest.raises(ValueError):
         Server(budget_bytes=1 << 20, lane_factory=lambda mt, ns: FakeLane(mt, ns)).run([big])
+
+
+def test_least_work_first_among_arrived_requests():
+    """With room for one simulation at a time, the requests waiting when a slot frees are
+    admitted in order of particles x steps; with "fifo", in arrival order."""
+    reqs = [Request(i, 0.0, configs.cell_sorting(n=n, side=12.0, seed=i), steps)
+            for i, (n, steps) in enumerate([(800, 20), (900, 30), (300, 5), (600, 4), (700, 40)])]
+    srv = Server(max_particles=1000, quantum=64, lane_factory=lambda mt, ns: FakeLane(mt, ns))
+    done = srv.run(reqs)
+    order = [r.rid for r in sorted(done, key=lambda r: (r.t_admit, r.rid))]
+    assert order == sorted(range(5), key=lambda i: reqs[i].workload.n * reqs[i].steps)
+    reqs2 = [Request(r.rid, 0.0, r.workload, r.steps) for r in reqs]
+    srv = Server(max_particles=1000, quantum=64, lane_factory=lambda mt, ns: FakeLane(mt, ns), policy="fifo")
+    done = srv.run(reqs2)
+    assert [r.rid for r in sorted(done, key=lambda r: (r.t_admit, r.rid))] == list(range(5))
+    for r in done:
+        assert r.result["steps"] == r.steps

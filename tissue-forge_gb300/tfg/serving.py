@@ -6,16 +6,19 @@ arena, tfg_batch_*) per model family -- simulations of one batch share their typ
 and species count -- and every batch runs on its own CUDA stream, so the families' steps
 overlap on the device.
 
-Admission is first come, first served, under two limits: an HBM byte budget (the arena
-footprint of a simulation, estimated per particle and per cell) and a cap on particles in
-flight (past the point where the GPU is full, more simulations only share it more thinly
-and every latency grows).  A batch advances in chunks of at most `quantum` steps, cut
+Admission runs under two limits: an HBM byte budget (the arena footprint of a simulation,
+estimated per particle and per cell) and a cap on particles in flight (past the point where
+the GPU is full, more simulations only share it more thinly and every latency grows).  Among
+the requests that have arrived, the default policy admits the least work first (particles x
+steps), so that a short request does not wait behind long ones that share the GPU; the
+"fifo" policy admits in arrival order.  A batch advances in chunks of at most `quantum` steps, cut
 short so that no simulation runs past its step count.  At a chunk boundary the finished
 simulations are downloaded and removed; requests that arrived meanwhile were already
 added (host-side) and join at the next chunk, without waiting for the batch to drain.
 Latency is completion time minus arrival time.
 """
 import collections
+import heapq
 import time
 
 import numpy as np
@@ -119,8 +122,11 @@ class Lane:
 class Server:
     """Continuous-batching request loop over one GPU (see the module docstring)."""
 
-    def __init__(self, budget_bytes=150 << 30, max_particles=4_000_000, quantum=50, device=0,
-                 keep_results=True, lane_factory=None):
+    def __init__(self, budget_bytes=150 << 30, max_particles=2_000_000, quantum=50, device=0,
+                 keep_results=True, lane_factory=None, policy="sjf"):
+        if policy not in ("sjf", "fifo"):
+            raise ValueError("policy is 'sjf' or 'fifo'")
+        self.policy = policy
         self.budget = int(budget_bytes)
         self.max_particles = int(max_particles)
         self.quantum = int(quantum)
@@ -155,10 +161,15 @@ class Server:
         clock = clock or (lambda: time.perf_counter() - t0)
         finished = []
         total = len(pending)
+        arrived = []   # heap of (priority, arrival, id, request)
         while len(finished) < total:
             now = clock()
-            while pending and pending[0].t_arrival <= now and self._fits(pending[0].workload):
+            while pending and pending[0].t_arrival <= now:
                 r = pending.popleft()
+                key = r.workload.n * r.steps if self.policy == "sjf" else 0
+                heapq.heappush(arrived, (key, r.t_arrival, r.rid, r))
+            while arrived and self._fits(arrived[0][3].workload):
+                r = heapq.heappop(arrived)[3]
                 self._lane(r.workload).admit(r)
                 r.t_admit = clock()
                 self.bytes_in_flight += footprint(r.workload)
@@ -173,6 +184,8 @@ class Server:
             if not running:
                 if pending:
                     sleep(max(0.0, min(0.01, pending[0].t_arrival - clock())))
+                elif arrived and not any(l.active for l in self.lanes.values()):
+                    raise RuntimeError("request %r cannot be admitted" % arrived[0][3].rid)
                 continue
             progressed = False
             for lane in running:
