@@ -25,7 +25,7 @@ namespace tfg {
 namespace {
 
 constexpr int kWarps = 8;
-constexpr int kCapT = 160;          // staged particles per warp (table variants)
+constexpr int kCapT = 156;          // staged particles per warp (table variants; 4 CTAs per SM)
 constexpr int kCapX = 104;          // staged particles per warp (DPD and flux variants)
 constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
 constexpr int kQ = 64;              // candidate ring queue entries per warp (power of two)
@@ -35,20 +35,27 @@ constexpr int kMaxSmemPots = 64;    // potential descriptors staged per CTA (all
 
 // One warp's staging area.  The DPD and flux variants (EXTRA) also stage each particle's
 // velocity, id, species value and flux increment, with fewer particles per warp so that
-// three CTAs still fit an SM.
+// three CTAs still fit an SM; the table variants fit four.
 template <int CAP, bool EXTRA> struct StagedT {
     static constexpr int cap = CAP;
     float4 pos[CAP];        // cell-relative position; w = type bits
     float4 acc[CAP];        // fx, fy, fz, number density (signature: count, hash bits)
     int32_t gslot[CAP];     // global slot of the staged particle
-    float4 sh4[CAP];        // shift of the staged particle's cell as seen from the home cell; w = radius
+    float rad[CAP];         // radius
     float sh[27][3];        // shift of each task's partner cell (space_getsid)
     uint32_t q[kQ];         // packed hit (i | k << 16), staged indices
     float4 vel[EXTRA ? CAP : 1];
     int32_t id[EXTRA ? CAP : 1];
     float sv[EXTRA ? CAP : 1];   // species 0 value
     float sq[EXTRA ? CAP : 1];   // species 0 flux increment
+    uint8_t seg[CAP];       // task of the staged particle's cell: its shift is sh[seg]
 };
+
+// Shift of staged particle k's cell as seen from the home cell, with its radius in w.
+template <class ST> __device__ __forceinline__ float4 staged_shift(const ST &S, int k) {
+    const float *s = S.sh[S.seg[k]];
+    return make_float4(s[0], s[1], s[2], S.rad[k]);
+}
 template <bool kDPD, bool kFlux> struct TileOf {
     using S = StagedT<(kDPD || kFlux) ? kCapX : kCapT, kDPD || kFlux>;
 };
@@ -82,7 +89,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
                                           float4 &fK, float &qI, float &qK) {
     const PairKernelArgs &a = T.a;
     const float4 pi = S.pos[I], pk = S.pos[K];
-    const float4 s4 = S.sh4[K];
+    const float4 s4 = staged_shift(S, K);
     const float3 sh = make_float3(s4.x, s4.y, s4.z);
     float3 dx;
     const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z), sh, make_float3(pk.x, pk.y, pk.z), dx);
@@ -126,7 +133,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
     if (pot.kind == POT_TABLE) {
         float e, f;
         // radii ride in the staged shift's w component
-        if (table_eval(pot, blob, S.sh4[I].w, s4.w, r2, e, f)) {
+        if (table_eval(pot, blob, S.rad[I], s4.w, r2, e, f)) {
             const float wx = f * dx.x, wy = f * dx.y, wz = f * dx.z;
             fI.x -= wx; fI.y -= wy; fI.z -= wz;
             fK.x += wx; fK.y += wy; fK.z += wz;
@@ -136,7 +143,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
     } else if (kDPD && pot.kind == POT_DPD) {
         float rr = r;
         const float ro = r < 1.1920928955078125e-7f ? 1.1920928955078125e-7f : r;
-        if (pot.flags & TFG_POTENTIAL_SHIFTED) rr = __fsub_rn(rr, __fadd_rn(S.sh4[I].w, s4.w));
+        if (pot.flags & TFG_POTENTIAL_SHIFTED) rr = __fsub_rn(rr, __fadd_rn(S.rad[I], s4.w));
         if (rr <= pot.b) {
             rr = rr >= pot.a ? rr : pot.a;
             const float4 vi = S.vel[I], vk = S.vel[K];
@@ -171,7 +178,7 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P
     if (kSig) {
         if (active) {
             // the pair decision proper (the table loop queues candidates with a looser filter)
-            const float4 pi = S.pos[I], pk = S.pos[K], s4 = S.sh4[K];
+            const float4 pi = S.pos[I], pk = S.pos[K], s4 = staged_shift(S, K);
             float3 dx;
             if (pair_r2(make_float3(pi.x, pi.y, pi.z), make_float3(s4.x, s4.y, s4.z), make_float3(pk.x, pk.y, pk.z),
                         dx) > P.cutoff2)
@@ -289,7 +296,8 @@ __device__ __forceinline__ void stage_body(const PairKernelArgs &a, ST &S, int b
         S.pos[base + k] = a.pos[g];
         S.acc[base + k] = make_float4(0.f, 0.f, 0.f, 0.f);
         S.gslot[base + k] = g;
-        S.sh4[base + k] = make_float4(S.sh[task][0], S.sh[task][1], S.sh[task][2], ax.x);
+        S.rad[base + k] = ax.x;
+        S.seg[base + k] = (uint8_t)task;
         if (!kSig && kDPD) {
             S.vel[base + k] = a.vel[g];
             S.id[base + k] = __float_as_int(ax.w);
@@ -351,7 +359,7 @@ __device__ __forceinline__ void flush(const PairKernelArgs &a, ST &S, int b0, in
 // those lists instead of testing every candidate pair (engine_flag_verlet; the reference
 // keeps its sorted windows between rebuilds instead, tf_runner_dopair.cpp:115-117).
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false>
-__global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
+__global__ void __launch_bounds__(kWarps * 32, (kDPD || kFlux) ? 3 : 4) k_pair_tile(TileArgs T) {
     using Staged = typename TileOf<kDPD, kFlux>::S;
     constexpr int kCap = Staged::cap;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -450,7 +458,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                 const int g = S.gslot[k];
                 float3 fw = make_float3(0.f, 0.f, 0.f);
                 float ew = 0.f;
-                wall_eval(P, a.wpots, blob, __float_as_int(p4.w), make_float3(p4.x, p4.y, p4.z), S.sh4[k].w,
+                wall_eval(P, a.wpots, blob, __float_as_int(p4.w), make_float3(p4.x, p4.y, p4.z), S.rad[k],
                           a.vel[g], __float_as_int(a.aux[g].w) - P.id_off, li, lj, lk, fw, ew);
                 S.acc[k].x += fw.x;
                 S.acc[k].y += fw.y;
@@ -504,7 +512,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                         const int I = e & 0xffff, K = e >> 16;
                         bool hit = false;
                         if (lane < fm && I < end && K < end) {
-                            const float4 pi4 = S.pos[I], pk = S.pos[K], s4 = S.sh4[K];
+                            const float4 pi4 = S.pos[I], pk = S.pos[K], s4 = staged_shift(S, K);
                             float3 dx;
                             const float r2 = pair_r2(make_float3(pi4.x, pi4.y, pi4.z), make_float3(s4.x, s4.y, s4.z),
                                                      make_float3(pk.x, pk.y, pk.z), dx);
@@ -548,7 +556,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                                 float4 pk = make_float4(0.f, 0.f, 0.f, 0.f), s4 = pk;
                                 if (k < end) {
                                     pk = S.pos[k];
-                                    s4 = S.sh4[k];
+                                    s4 = staged_shift(S, k);
                                 }
                                 ilim = k < end ? (k < nh ? k : nh) : 0;
                                 iend = kb + 31 < nh ? kb + 31 : nh;
@@ -590,7 +598,7 @@ __global__ void __launch_bounds__(kWarps * 32, 3) k_pair_tile(TileArgs T) {
                         float4 pk = make_float4(0.f, 0.f, 0.f, 0.f), s4 = pk;
                         if (k < end) {
                             pk = S.pos[k];
-                            s4 = S.sh4[k];
+                            s4 = staged_shift(S, k);
                         }
                         const int ilim = k < end ? (k < nh ? k : nh) : 0;
                         const int iend = kb + 31 < nh ? kb + 31 : nh;
