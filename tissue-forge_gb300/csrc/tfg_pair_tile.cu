@@ -25,8 +25,8 @@ namespace tfg {
 namespace {
 
 constexpr int kWarps = 8;
-constexpr int kCapT = 156;          // staged particles per warp (table variants; 4 CTAs per SM)
-constexpr int kCapX = 104;          // staged particles per warp (DPD and flux variants)
+constexpr int kCapT = 156;          // staged particles per warp (table variants)
+constexpr int kCapX = 88;           // staged particles per warp (DPD and flux variants)
 constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
 constexpr int kQ = 64;              // candidate ring queue entries per warp (power of two)
 constexpr int kGrab = 1;            // work items a warp takes from the shared counter at a time
@@ -34,8 +34,8 @@ constexpr int kMaxSmemTable = 4096; // floats of potential table staged per CTA
 constexpr int kMaxSmemPots = 64;    // potential descriptors staged per CTA (all simulations)
 
 // One warp's staging area.  The DPD and flux variants (EXTRA) also stage each particle's
-// velocity, id, species value and flux increment, with fewer particles per warp so that
-// three CTAs still fit an SM; the table variants fit four.
+// velocity, id, species value and flux increment, with fewer particles per warp, so that
+// every variant fits four CTAs per SM.
 template <int CAP, bool EXTRA> struct StagedT {
     static constexpr int cap = CAP;
     float4 pos[CAP];        // cell-relative position; w = type bits
@@ -359,7 +359,7 @@ __device__ __forceinline__ void flush(const PairKernelArgs &a, ST &S, int b0, in
 // those lists instead of testing every candidate pair (engine_flag_verlet; the reference
 // keeps its sorted windows between rebuilds instead, tf_runner_dopair.cpp:115-117).
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false>
-__global__ void __launch_bounds__(kWarps * 32, (kDPD || kFlux) ? 3 : 4) k_pair_tile(TileArgs T) {
+__global__ void __launch_bounds__(kWarps * 32, 4) k_pair_tile(TileArgs T) {
     using Staged = typename TileOf<kDPD, kFlux>::S;
     constexpr int kCap = Staged::cap;
     extern __shared__ __align__(16) unsigned char smem_raw[];
