@@ -32,6 +32,7 @@ constexpr int kQ = 64;              // candidate ring queue entries per warp (po
 constexpr int kGrab = 1;            // work items a warp takes from the shared counter at a time
 constexpr int kMaxSmemTable = 4096; // floats of potential table staged per CTA
 constexpr int kMaxSmemPots = 64;    // potential descriptors staged per CTA (all simulations)
+constexpr size_t kFourCtaBytes = 228 * 1024 / 4 - 1024;   // dynamic shared memory of a CTA, four per SM
 
 // One warp's staging area.  The DPD and flux variants (EXTRA) also stage each particle's
 // velocity, id, species value and flux increment, with fewer particles per warp, so that
@@ -794,9 +795,17 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
 }
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false>
-void launch_variant(const TileArgs &T, cudaStream_t s, int sms) {
+void launch_variant(const TileArgs &T0, cudaStream_t s, int sms) {
     const size_t base = sizeof(typename TileOf<kDPD, kFlux>::S) * kWarps;
     const size_t smem_max = base + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxSmemPots;
+    // Tables and descriptors are staged only while a CTA still fits four per SM: the fourth
+    // CTA is worth more than shared-memory tables (the table variants' staging alone takes
+    // 56 KB, so their tables are always read through L1)
+    TileArgs T = T0;
+    if (base + sizeof(PotDev) * T.stage_pots + sizeof(float) * ((T.stage_floats + 3) & ~3) > kFourCtaBytes) {
+        T.stage_floats = 0;
+        T.stage_pots = 0;
+    }
     const size_t smem = base + sizeof(PotDev) * T.stage_pots + sizeof(float) * ((T.stage_floats + 3) & ~3);
     static bool configured = false;
     static size_t occ_smem = 0;
