@@ -51,6 +51,53 @@ __device__ __forceinline__ void keyed_add(double *red, int rb, int slot, float v
     }
 }
 
+// keyed_add of three values to three slots of the same simulation, under one set of block
+// barriers.
+__device__ __forceinline__ void keyed_add3(double *red, int rb, int s0, float v0, int s1, float v1, int s2, float v2) {
+    __shared__ double part3[3][32];
+    const int rb0 = __shfl_sync(0xffffffffu, rb, 0);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __shared__ int block_rb3;
+    if (threadIdx.x == 0) block_rb3 = rb;
+    __syncthreads();
+    const bool uniform = __syncthreads_and(rb == block_rb3 || rb < 0);
+    float a = v0, b = v1, c = v2;
+    if (uniform || __all_sync(0xffffffffu, rb == rb0 || rb < 0)) {
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(0xffffffffu, a, o);
+            b += __shfl_down_sync(0xffffffffu, b, o);
+            c += __shfl_down_sync(0xffffffffu, c, o);
+        }
+    }
+    if (uniform) {
+        if (lane == 0) {
+            part3[0][w] = (double)a;
+            part3[1][w] = (double)b;
+            part3[2][w] = (double)c;
+        }
+        __syncthreads();
+        if (threadIdx.x < 3 && block_rb3 >= 0) {
+            double t = 0.0;
+            for (int k = 0; k < nw; k++) t += part3[threadIdx.x][k];
+            const int slot = threadIdx.x == 0 ? s0 : (threadIdx.x == 1 ? s1 : s2);
+            if (t != 0.0) atomicAdd(&red[block_rb3 + slot], t);
+        }
+        __syncthreads();
+        return;
+    }
+    if (__all_sync(0xffffffffu, rb == rb0 || rb < 0)) {
+        if (lane == 0 && rb0 >= 0) {
+            if (a != 0.f) atomicAdd(&red[rb0 + s0], (double)a);
+            if (b != 0.f) atomicAdd(&red[rb0 + s1], (double)b);
+            if (c != 0.f) atomicAdd(&red[rb0 + s2], (double)c);
+        }
+    } else if (rb >= 0) {
+        if (v0 != 0.f) atomicAdd(&red[rb + s0], (double)v0);
+        if (v1 != 0.f) atomicAdd(&red[rb + s1], (double)v1);
+        if (v2 != 0.f) atomicAdd(&red[rb + s2], (double)v2);
+    }
+}
+
 __global__ void k_stamp(unsigned long long *t, int k) {
     unsigned long long v;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(v));
@@ -344,8 +391,7 @@ __global__ void k_bonds(int nb, const SimParams *sims, const int32_t *cell_sim, 
             }
         }
     }
-    keyed_add(red, rb, RED_EPOT_BOND, epot);
-    keyed_add(red, rb, RED_VIRIAL, vir);
+    keyed_add3(red, rb, RED_EPOT_BOND, epot, RED_VIRIAL, vir, RED_VIRIAL, 0.f);
 }
 
 // angle_eval (tfAngle.cpp:90-382); one thread per angle, j is the vertex.
@@ -577,9 +623,7 @@ reduce:
             atomicMax(&sims[vsim].verlet_maxdx2, dx2);
         }
     }
-    keyed_add(red, rb, RED_KINETIC, ke);
-    keyed_add(red, rb, RED_VOLUME, vol);
-    keyed_add(red, rb, RED_MIGRATIONS, mig);
+    keyed_add3(red, rb, RED_KINETIC, ke, RED_VOLUME, vol, RED_MIGRATIONS, mig);
     for (int s = 0; s < nspec; s++) keyed_add(red, rb, RED_SPECIES0 + s, stot[s]);
 }
 
