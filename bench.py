@@ -207,8 +207,9 @@ def hbm_peak():
 
 
 def clock_path(name):
-    d = os.path.join(ROOT, "gpurun_out")
-    return os.path.join(d if os.path.isdir(d) else "/tmp", name)
+    """Where the nvidia-smi clock samples go (TFG_CLOCKS_DIR, else the temporary directory)."""
+    import tempfile
+    return os.path.join(os.environ.get("TFG_CLOCKS_DIR") or tempfile.gettempdir(), name)
 
 
 def fp32_peak(dev):
