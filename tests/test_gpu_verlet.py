@@ -209,3 +209,32 @@ def test_full_size_list_walk_equals_candidate_tests():
     assert int(gc.sum()) // 2 > 50_000_000
     dev = _dev(g.download()["x"], h.download()["x"], w.dim)
     assert dev.max() < 1e-3
+
+
+def test_membership_change_forces_a_rebuild():
+    """Adding a simulation to a batch re-lays the arena out, which rebuilds every Verlet member
+    at the next step (cells, reference positions and pair lists are taken afresh).  The member
+    then follows the oracle with a rebuild forced at the same step."""
+    w = configs.verlet(configs.cell_sorting(n=2500, side=17.0, seed=41, random_force=(0.0, 2.0, 1)), skin=0.3)
+    other = configs.cell_sorting(n=900, side=12.5, seed=42)
+    b = Batch(w.max_type, w.nr_species)
+    s = b.add_sim(w.desc())
+    b._keep.extend(setup_model(s, w))
+    o = make_oracle(w)
+    b.step(6)
+    o.step(6)
+    assert s.verlet()[0] == o.verlet()[0]
+    s2 = b.add_sim(other.desc())
+    b._keep.extend(setup_model(s2, other))
+    o.set_boundary(0, abi.BOUNDARY_PERIODIC)     # the oracle's way to force the next step's rebuild
+    before = s.verlet()[0]
+    b.step(1)
+    o.step(1)
+    assert s.verlet()[0] == before + 1 == o.verlet()[0]
+    b.step(5)
+    o.step(5)
+    assert s.verlet()[0] == o.verlet()[0]
+    a, r = s.download(), o.download()
+    assert np.array_equal(a["cell"], r["cell"])
+    dev = _dev(a["x"], r["x"], w.dim)
+    assert dev.max() < 2e-3 and np.percentile(dev, 99) < 1e-4
