@@ -378,17 +378,26 @@ TFG_API int tfg_probe_fp32_tflops(int device, double *tflops);
  * `cell_start` (ncells+1 offsets into `order`).  It calls no cudaMalloc, cudaFree or
  * allocating library routine: its temporaries live in one file-scope device array of
  * TFG_NOALLOC_SCRATCH_BYTES that every GPU loading this library holds until exit.
- *   - Limits: n <= TFG_NOALLOC_MAX_PARTICLES and cells[0]*cells[1]*cells[2] <=
- *     TFG_NOALLOC_MAX_CELLS; larger requests return TFG_E_OVERFLOW and do nothing.
- *   - The first call on a device looks up the array's device address (cudaGetSymbolAddress
- *     with that device current); make that first call before any stream capture.
- *   - All calls share the one array: calls whose work overlaps on the GPU (other streams,
- *     other host threads) race.  Serialise them, e.g. on one stream.
+ *   - Limits: n <= TFG_NOALLOC_MAX_PARTICLES, every cells[k] and the product
+ *     cells[0]*cells[1]*cells[2] <= TFG_NOALLOC_MAX_CELLS; larger requests return
+ *     TFG_E_OVERFLOW and do nothing.  Any cells[k] >= 1 is accepted.
+ *   - Work is linear in n however the particles are spread (a stable radix sort on the
+ *     cell index): all of them in one cell costs what a uniform spread costs.
+ *   - The first call in a CUDA context looks up the array's device address
+ *     (cudaGetSymbolAddress, with the device current) and keeps it for that context; make
+ *     that first call before any stream capture.  A context created later (the host
+ *     application's own, or the primary context after cudaDeviceReset) gets its own lookup.
+ *   - All calls share the one array, and each call clears what must start at zero: calls
+ *     whose work overlaps on the GPU (other streams, other host threads) race.  Serialise
+ *     them, e.g. on one stream.
  *   - Work is queued on `stream` (a cudaStream_t; NULL = legacy default stream).
+ *   - TFG_E_CUDA reports a failure of this call's own launches only: earlier errors on the
+ *     calling thread are neither read nor cleared (no cudaGetLastError).
  * No counterpart in the reference (its binning always runs on the host). */
 #define TFG_NOALLOC_MAX_PARTICLES 1048576
 #define TFG_NOALLOC_MAX_CELLS     262144
-#define TFG_NOALLOC_SCRATCH_BYTES ((TFG_NOALLOC_MAX_CELLS + 2 * TFG_NOALLOC_MAX_PARTICLES + 256) * 4)
+#define TFG_NOALLOC_SCRATCH_BYTES \
+    ((TFG_NOALLOC_MAX_CELLS + 2 * 256 * (TFG_NOALLOC_MAX_PARTICLES / 1024) + 1 + 2 * TFG_NOALLOC_MAX_PARTICLES + 256) * 4)
 TFG_API int tfg_bin_noalloc(const tfg_engine_desc *desc, int n, const float *x_dev, int32_t *cell_dev,
                             float *xrel_dev, int32_t *order_dev, int32_t *cell_start_dev, void *stream);
 
