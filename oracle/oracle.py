@@ -3,7 +3,8 @@
 TEST INFRASTRUCTURE ONLY: the oracle is the checker of the GPU engine.  Only the
 tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.  It
 restates the reference's mdcore CPU engine; see tfg_oracle.cpp for the file:line
-map.  Parity is unpinned by the reference (which cannot be built here and holds no
+map.  It builds its own potential tables (tfo_potential.cpp, a restatement of
+tfPotential.cpp's potential_init and factories) and never loads the product library.  Parity is unpinned by the reference (which cannot be built here and holds no
 golden vectors for this path); it is pinned by known-answer tests and by the
 fixtures under tests/golden/.
 """
@@ -27,14 +28,19 @@ MODE_REF_DPD_RANDOM = 4
 MODE_NO_DENSITY = 8
 
 
+SOURCES = ("tfg_oracle.cpp", "tfo_potential.cpp")
+
+
 def build(force=False):
     """Compile the oracle with the reference's FP rules (no FMA contraction)."""
-    src = os.path.join(HERE, "tfg_oracle.cpp")
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
+    deps = srcs + [os.path.join(ROOT, "include", "tfg.h")]
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+    if not force and os.path.exists(LIB_PATH) and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(d)
+                                                      for d in deps):
         return LIB_PATH
     cmd = ["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-           "-I" + os.path.join(ROOT, "include"), "-o", LIB_PATH, src, "-lpthread"]
+           "-I" + os.path.join(ROOT, "include"), "-o", LIB_PATH, *srcs, "-lpthread"]
     subprocess.check_call(cmd)
     return LIB_PATH
 
@@ -82,6 +88,15 @@ def lib():
         L.tfo_get_pairs.restype = C.c_int64
         L.tfo_philox_probe.argtypes = [C.c_uint32] * 6 + [C.POINTER(C.c_uint32)]
         L.tfo_philox_probe.restype = C.c_uint32
+        PP = C.POINTER(abi.P_POT)
+        f = C.c_float
+        L.tfo_potential_morse.argtypes = [f, f, f, f, f, f, C.c_int, PP]
+        L.tfo_potential_lennard_jones_12_6.argtypes = [f, f, f, f, f, PP]
+        L.tfo_potential_harmonic.argtypes = [f, f, f, f, f, PP]
+        L.tfo_potential_harmonic_angle.argtypes = [f, f, f, f, f, PP]
+        L.tfo_potential_dpd.argtypes = [f, f, f, f, C.c_int, PP]
+        L.tfo_potential_free.argtypes = [abi.P_POT]
+        L.tfo_potential_free.restype = None
     return _lib
 
 
@@ -100,6 +115,69 @@ def _up(a):
 def _chk(rc, what):
     if rc != 0:
         raise RuntimeError("oracle %s failed: %s" % (what, abi.STATUS_NAMES.get(rc, rc)))
+
+
+class OraclePotential:
+    """A potential table built by the oracle's own restatement of the reference's
+    potential_init and factories (tfo_potential.cpp), never by the product library."""
+
+    def __init__(self, ptr, kind):
+        self.ptr = ptr
+        self.kind = kind
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                lib().tfo_potential_free(self.ptr)
+                self.ptr = None
+        except Exception:
+            pass
+
+    @property
+    def n(self):
+        return self.ptr.contents.n
+
+    def table(self):
+        """(kind, flags, alpha[4], r0_plusone, a, b, n, c as float32 array or None)."""
+        p = self.ptr.contents
+        c = None
+        if p.c:
+            c = np.ctypeslib.as_array(p.c, shape=((p.n + 1) * 8,)).copy()
+        return (p.kind, p.flags, tuple(p.alpha), p.r0_plusone, p.a, p.b, p.n, c)
+
+    @classmethod
+    def _make(cls, fn, *args, kind):
+        p = abi.P_POT()
+        rc = fn(*args, C.byref(p))
+        if rc != 0:
+            raise ValueError("oracle %s failed: %s" % (kind, abi.STATUS_NAMES.get(rc, rc)))
+        return cls(p, kind)
+
+    @classmethod
+    def from_spec(cls, spec):
+        """Build the potential a configs.PotSpec names (factory arguments, or a stored table)."""
+        a = spec.args
+        L = lib()
+        if spec.kind == "table":
+            from tfg.potentials import RawPotential   # holds a given table; builds nothing
+            return RawPotential(a["kind"], a["flags"], a["alpha"], a["r0_plusone"], a["a"], a["b"], a["n"],
+                                a["c"], a.get("dpd", (0.0, 0.0, 0.0)))
+        if spec.kind == "morse":
+            return cls._make(L.tfo_potential_morse, a["d"], a["a"], a["r0"], a["min"], a["max"], a["tol"],
+                             1 if a["shifted"] else 0, kind="morse")
+        if spec.kind == "lj":
+            return cls._make(L.tfo_potential_lennard_jones_12_6, a["min"], a["max"], a["A"], a["B"], a["tol"],
+                             kind="lj")
+        if spec.kind == "harmonic":
+            return cls._make(L.tfo_potential_harmonic, a["k"], a["r0"], a["min"], a["max"], a["tol"],
+                             kind="harmonic")
+        if spec.kind == "harmonic_angle":
+            return cls._make(L.tfo_potential_harmonic_angle, a["k"], a["theta0"], a["min"], a["max"], a["tol"],
+                             kind="harmonic_angle")
+        if spec.kind == "dpd":
+            return cls._make(L.tfo_potential_dpd, a["alpha"], a["gamma"], a["sigma"], a["cutoff"],
+                             1 if a["shifted"] else 0, kind="dpd")
+        raise ValueError(spec.kind)
 
 
 class OracleEngine:
@@ -127,6 +205,11 @@ class OracleEngine:
 
     def set_type(self, t, dynamics, mass=1.0):
         _chk(self.L.tfo_set_type(self.h, t, dynamics, mass), "set_type")
+
+    @staticmethod
+    def potential_from_spec(spec):
+        """The oracle builds its own tables (setup_model calls this when present)."""
+        return OraclePotential.from_spec(spec)
 
     def set_potential(self, ti, tj, pot):
         _chk(self.L.tfo_set_potential(self.h, ti, tj, pot), "set_potential")

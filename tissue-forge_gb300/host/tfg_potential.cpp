@@ -8,6 +8,12 @@
 // where the reference's C++ expressions promote to double, and no FMA contraction
 // (this file is compiled with -ffp-contract=off).
 //
+// Promotion rule: tfPotential.cpp includes <cmath> but never <math.h>, so its
+// unqualified fabs/sqrt/cos/acos calls on float arguments resolve to the C library's
+// double functions; only explicitly qualified std:: calls (Power(), std::sqrt in
+// DPDPotential) take the float overloads.  The domain stretch, the transform correction
+// and the harmonic-angle interpoland below therefore compute in double.
+//
 // Steps restated (same order, same arithmetic types):
 //   node density transform        potential_getalpha      tfPotential.cpp:1977-2040
 //   node placement (Newton)                               tfPotential.cpp:1457-1465
@@ -254,17 +260,21 @@ real node_alpha(const Interpoland &I, real a, real b) {
 
 // Nodes xi[0..n] of the transform t(x) = alpha0 + x*(alpha1 + x*alpha2), placed at
 // t = i/n by Newton iteration.
-void place_nodes(const real *alpha, real a, real b, int n, real *xi) {
+// The reference iterates without a bound; a table whose iteration has not converged
+// after 100,000 steps is refused instead of hanging the host.
+bool place_nodes(const real *alpha, real a, real b, int n, real *xi) {
     const real mtol = 10 * FLT_EPSILON;
     xi[0] = a; xi[n] = b;
     for (int i = 1; i < n; i++) {
         xi[i] = a + (b - a) * i / n;
-        for (;;) {
+        for (int it = 0;; it++) {
             real e = i - n * (alpha[0] + xi[i] * (alpha[1] + xi[i] * alpha[2]));
             xi[i] += e / (n * (alpha[1] + 2 * xi[i] * alpha[2]));
-            if (std::fabs(e) < n * mtol) break;
+            if (std::fabs((double)e) < n * mtol) break;
+            if (it > 100000) return false;
         }
     }
+    return true;
 }
 
 struct Table {
@@ -275,9 +285,12 @@ struct Table {
 // One interpolation with n intervals: returns its error and fills t.
 real build_with(const Interpoland &I, const real *alpha, real a, real b, int n, Table &t) {
     std::vector<real> xi(n + 1);
-    place_nodes(alpha, a, b, n, xi.data());
     t.n = n;
     t.c.assign((size_t)(n + 1) * kChunk, 0.0f);
+    if (!place_nodes(alpha, a, b, n, xi.data())) {
+        t.n = -1;
+        return INFINITY;
+    }
     return interval_coefficients(I, xi.data(), n, t.c.data() + kChunk);
 }
 
@@ -310,8 +323,8 @@ struct Built {
 Built init_table(const Interpoland &I, real a, real b, real tol) {
     Built out;
     out.a = a; out.b = b;
-    b += std::fabs(b) * std::sqrt(FLT_EPSILON);
-    a -= std::fabs(a) * std::sqrt(FLT_EPSILON);
+    b = (real)(b + std::fabs((double)b) * std::sqrt((double)FLT_EPSILON));
+    a = (real)(a - std::fabs((double)a) * std::sqrt((double)FLT_EPSILON));
 
     real al = node_alpha(I, a, b);
     real *A = out.alpha;
@@ -321,13 +334,14 @@ Built init_table(const Interpoland &I, real a, real b, real tol) {
     A[1] = -2 * a * w + al * (a + b) * w;
     A[2] = w - al * w;
     A[3] = 0.0;
-    w = 2 * FLT_EPSILON * (std::fabs(A[0]) + std::fabs(A[1]) + std::fabs(A[2]));
+    w = (real)(2 * FLT_EPSILON * (std::fabs((double)A[0]) + std::fabs((double)A[1]) + std::fabs((double)A[2])));
     A[0] -= w * a / (a - b);
     A[1] += w / (a - b);
 
     int l = kIvalsA, r = kIvalsB;
     Table tl, tr;
     real err_l = build_with(I, A, a, b, l, tl);
+    if (tl.n < 0) { out.status = TFG_E_INVAL; return out; }
     Table *chosen = nullptr;
     if (err_l < tol) {
         chosen = &tl;
@@ -335,6 +349,7 @@ Built init_table(const Interpoland &I, real a, real b, real tol) {
         // Double the right bracket until it meets the tolerance.
         for (;;) {
             real err_r = build_with(I, A, a, b, r, tr);
+            if (tr.n < 0) { out.status = TFG_E_INVAL; return out; }
             if (err_r < tol) break;
             if (2 * r > kIvalsMax) { out.status = TFG_E_OVERFLOW; return out; }
             l = r; tl = tr;
@@ -345,6 +360,7 @@ Built init_table(const Interpoland &I, real a, real b, real tol) {
             int m = 0.5 * (r + l);
             Table tm;
             real err_m = build_with(I, A, a, b, m, tm);
+            if (tm.n < 0) { out.status = TFG_E_INVAL; return out; }
             if (err_m > tol) { l = m; tl = std::move(tm); }
             else { r = m; tr = std::move(tm); }
         }
@@ -432,7 +448,8 @@ TFG_API int tfg_potential_lennard_jones_12_6(float min, float max, float A, floa
         return (real)(10080.0 * ir12 * (884.0 * A * ir6 - 33.0 * B));
     };
     Built b = init_table(I, min, max, tol);
-    return publish(b, TFG_POTENTIAL_R2 | TFG_POTENTIAL_LJ126, 0.0f, out);
+    // r0_plusone keeps Potential's default 1 (tfPotential.cpp:63); LJ is not shifted.
+    return publish(b, TFG_POTENTIAL_R2 | TFG_POTENTIAL_LJ126, 1.0f, out);
 }
 
 TFG_API int tfg_potential_harmonic(float k, float r0, float min, float max, float tol,
@@ -456,22 +473,24 @@ TFG_API int tfg_potential_harmonic(float k, float r0, float min, float max, floa
 TFG_API int tfg_potential_harmonic_angle(float k, float theta0, float min, float max, float tol,
                                          tfg_potential **out) {
     if (!out) return TFG_E_INVAL;
-    if (min < 0) min = 0.0;
-    if (max < 0) max = M_PI;
-    if (tol <= 0) tol = 0.005 * (max - min);
-    real a = min, b = max;
+    // The wrapper's defaults are double literals, so its range and default tolerance are
+    // doubles (tfPotential.cpp:2995-2997) until they are passed on as FPTYPE.
+    const double lo = min < 0 ? 0.0 : (double)min;
+    const double hi = max < 0 ? M_PI : (double)max;
+    if (tol <= 0) tol = 0.005 * (hi - lo);
+    real a = lo, b = hi;
     if (a < 0.0) a = 0.0;
     if (b > M_PI) b = M_PI;
-    real left = std::cos(b), right = std::cos(a);
+    real left = std::cos((double)b), right = std::cos((double)a);
     Interpoland I;
     I.f = [=](real r) {
         r = std::fmin(1.0, std::fmax(-1.0, (double)r));
-        real theta = std::acos(r);
+        real theta = std::acos((double)r);
         return k * (theta - theta0) * (theta - theta0);
     };
     I.f6p = [](real) { return (real)0; };
     Built bt = init_table(I, left, right, tol);
-    return publish(bt, TFG_POTENTIAL_ANGLE | TFG_POTENTIAL_HARMONIC, 0.0f, out);
+    return publish(bt, TFG_POTENTIAL_ANGLE | TFG_POTENTIAL_HARMONIC, 1.0f, out);
 }
 
 TFG_API int tfg_potential_dpd(float alpha, float gamma, float sigma, float cutoff, int shifted,
@@ -482,6 +501,10 @@ TFG_API int tfg_potential_dpd(float alpha, float gamma, float sigma, float cutof
     std::memset(&op->pub, 0, sizeof(op->pub));
     op->pub.kind = TFG_POTENTIAL_KIND_DPD;
     op->pub.flags = shifted ? TFG_POTENTIAL_SHIFTED : 0u;
+    // Potential's defaults for the fields DPD leaves alone (tfPotential.cpp:59-81): n = 1,
+    // r0_plusone = 1; no table.
+    op->pub.n = 1;
+    op->pub.r0_plusone = 1.0f;
     op->pub.a = std::sqrt(FLT_EPSILON);
     op->pub.b = cutoff;
     op->pub.dpd_alpha = alpha;

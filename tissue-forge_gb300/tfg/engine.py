@@ -348,13 +348,15 @@ class Sim:
         return int(nb.value), float(m.value)
 
 
-def _potential(spec, cache):
+def _potential(spec, cache, factory=None):
+    make = factory or Potential.from_spec
     if cache is None:
-        return Potential.from_spec(spec)
-    key = (spec.kind, tuple(sorted((k, tuple(v) if isinstance(v, list) else v) for k, v in spec.args.items())))
+        return make(spec)
+    key = (getattr(make, "__qualname__", ""), spec.kind,
+           tuple(sorted((k, tuple(v) if isinstance(v, list) else v) for k, v in spec.args.items())))
     p = cache.get(key)
     if p is None:
-        p = cache[key] = Potential.from_spec(spec)
+        p = cache[key] = make(spec)
     return p
 
 
@@ -362,12 +364,14 @@ def setup_model(eng, w, keep=None, pot_cache=None):
     """Apply a configs.Workload's interaction model and particles to an engine-like object
     (the GPU Engine, a batch Sim, or the CPU oracle share these method names).  Returns the
     Potential objects, which must stay alive while the engine uses their tables.  With a
-    pot_cache dict, equal potential specifications share one table."""
+    pot_cache dict, equal potential specifications share one table.  An engine-like object
+    with a potential_from_spec method (the oracle) builds its own tables with it."""
     pots = []
+    factory = getattr(eng, "potential_from_spec", None)
     for t in range(w.max_type):
         eng.set_type(t, w.dynamics[t], w.mass[t])
     for (ti, tj), spec in w.pots.items():
-        p = _potential(spec, pot_cache)
+        p = _potential(spec, pot_cache, factory)
         pots.append(p)
         eng.set_potential(ti, tj, p.ptr)
     for (ti, tj, f) in w.fluxes:
@@ -381,19 +385,19 @@ def setup_model(eng, w, keep=None, pot_cache=None):
     for (wall, kind, vel, restore, radius) in w.boundaries:
         eng.set_boundary(wall, kind, vel, restore, radius)
     for (wall, t, spec) in w.wall_pots:
-        p = _potential(spec, pot_cache)
+        p = _potential(spec, pot_cache, factory)
         pots.append(p)
         eng.set_boundary_potential(wall, t, p.ptr)
     if w.bond_pot is not None:
-        p = _potential(w.bond_pot, pot_cache)
+        p = _potential(w.bond_pot, pot_cache, factory)
         pots.append(p)
         eng.set_bonded_potential(0, p.ptr)
     if w.angle_pot is not None:
-        p = _potential(w.angle_pot, pot_cache)
+        p = _potential(w.angle_pot, pot_cache, factory)
         pots.append(p)
         eng.set_bonded_potential(1, p.ptr)
     for slot, spec in enumerate(w.bonded_pots):
-        p = _potential(spec, pot_cache)
+        p = _potential(spec, pot_cache, factory)
         pots.append(p)
         eng.set_bonded_potential(slot, p.ptr)
     eng.load(w.x, v=w.v, type=w.type, radius=w.radius, imass=w.imass, flags=w.flags_particles, species=w.species,

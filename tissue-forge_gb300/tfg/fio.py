@@ -89,8 +89,9 @@ def _potential(node):
     if kind == _POTENTIAL_KIND_COMBINATION:
         raise ValueError("combined potentials are not supported")
     if kind == abi.POTENTIAL_KIND_DPD:   # DPDPotential (tfDPDPotential.cpp:66-80)
-        return PotSpec("table", dict(kind=kind, flags=flags, alpha=(0.0,) * 4, r0_plusone=0.0, a=_f(node["a"]),
-                                     b=_f(node["b"]), n=0, c=(),
+        # fields DPD does not store keep Potential's defaults (tfPotential.cpp:59-81)
+        return PotSpec("table", dict(kind=kind, flags=flags, alpha=(0.0,) * 4, r0_plusone=1.0, a=_f(node["a"]),
+                                     b=_f(node["b"]), n=1, c=(),
                                      dpd=(_f(node["alpha"]), _f(node["gamma"]), _f(node["sigma"]))))
     alpha = tuple(_vec(node["alpha"], _f))
     n = _i(node["n"])
