@@ -279,11 +279,16 @@ TFG_API int tfg_set_graphs(tfg_engine *eng, int enable);
  * next one; off, every step tests all candidate pairs of the cell stencil.  The pair set
  * is the same either way. */
 TFG_API int tfg_set_pair_lists(tfg_engine *eng, int enable);
-/* Autotune the nonbonded pass's work split (warps per home cell: 1, 2, 7 or 14) by timing
- * each choice on the current state; the state is left unchanged.  tfg_step and
- * tfg_force_only run it on their first call; tfg_set_split fixes the split instead.
- * The reference selects CUDA blocks/threads by hand (cuda::EngineConfig::setBlocks /
- * setThreads, source/cuda/tfEngineConfig.cpp:98-124). */
+/* Autotune the nonbonded pass's form by timing each choice on the current state; the
+ * state is left unchanged.  The choices are the tiled kernel's work split (warps per home
+ * cell: 1, 2, 7 or 14) and, for engines whose potentials are all tabulated (no DPD, no
+ * fluxes, no Verlet pair lists), TFG_PAIR_HOME_OUTER: the kernel that takes home particles
+ * one at a time against targets held in registers.  tfg_step and tfg_force_only run it on
+ * their first call; tfg_set_split fixes the choice instead (TFG_PAIR_HOME_OUTER falls back
+ * to split 1 while the engine is not eligible).  The reference selects CUDA
+ * blocks/threads by hand (cuda::EngineConfig::setBlocks / setThreads,
+ * source/cuda/tfEngineConfig.cpp:98-124). */
+#define TFG_PAIR_HOME_OUTER 32
 TFG_API int tfg_autotune(tfg_engine *eng, int *split);
 TFG_API int tfg_set_split(tfg_engine *eng, int split);
 /* Pair-set signature of the current binned state, per particle id: the number of
@@ -360,8 +365,101 @@ TFG_API int tfg_batch_download(tfg_engine *eng, int sim, float *x, float *xrel, 
                                float *f, float *density, float *species, float *q);
 TFG_API int tfg_batch_get_reductions(tfg_engine *eng, int sim, tfg_reductions *out);
 TFG_API int tfg_batch_get_verlet(tfg_engine *eng, int sim, int64_t *rebuilds, float *maxdx);
+/* Status of one simulation: TFG_OK, or the first error its particles raised (TFG_E_NAN,
+ * TFG_E_TOOFAST, TFG_E_RANGE), kept until the simulation is removed.  The reference flags
+ * the offending particle and fails the whole step (toofast_error,
+ * tf_engine_advance.cpp:72-85, 204-206); in a batch each simulation fails alone: the step
+ * call (or tfg_sync) that observes an error returns it, its message names the failed
+ * simulations, and the others are unaffected and keep stepping once the failed ones are
+ * removed (tfg_batch_remove_sim) or even while they stay.  Waits for the engine's stream. */
+TFG_API int tfg_batch_sim_status(tfg_engine *eng, int sim, int *status);
 TFG_API int tfg_batch_set_boundary(tfg_engine *eng, int sim, int wall, const tfg_boundary *bc);
 TFG_API int tfg_batch_set_boundary_potential(tfg_engine *eng, int sim, int wall, int type, const tfg_potential *p);
+
+/* ---- serving: continuous batching of simulation requests ----
+ * The reference runs one simulation per process; there is no counterpart to a server.  Its
+ * C entry style (handle + HRESULT-like status, wraps/C/tfC_cuda.h:117-125,
+ * wraps/C/tfCUniverse.h:153) is kept.  A request is a whole simulation recorded host-side
+ * (tfg_request_*: the same operations as a batch member) plus a step count.  The server keeps
+ * one batch (tfg_batch_*) per model family (max_type, nr_species), each on its own CUDA
+ * stream, admits arrived requests while they fit an HBM budget and a cap on particles in
+ * flight (least work, particles x steps, first; or first come, first served), advances each
+ * batch in chunks of at most `quantum` steps cut so that no simulation overshoots, and at
+ * every chunk boundary retires the finished simulations (results downloaded to host memory)
+ * and admits waiting requests: requests that arrive while others run join at the next chunk.
+ * A simulation whose particles raise an error (TFG_E_NAN, TFG_E_TOOFAST, TFG_E_RANGE) is
+ * retired as failed with that status; the rest of its batch continues.
+ * Threading: one host thread per server handle; tfg_server_poll does all device work. */
+typedef struct tfg_server tfg_server;
+typedef struct tfg_request tfg_request;
+
+#define TFG_SERVER_LEAST_WORK 0
+#define TFG_SERVER_FIFO       1
+
+#define TFG_REQ_QUEUED  0   /* submitted, waiting for admission */
+#define TFG_REQ_RUNNING 1   /* in a batch on the device */
+#define TFG_REQ_DONE    2   /* finished; its result is ready */
+#define TFG_REQ_FAILED  3   /* retired with an error status */
+
+typedef struct tfg_server_desc {
+    int32_t device;
+    int32_t quantum;          /* largest chunk of steps between admissions (0 -> 50) */
+    int64_t budget_bytes;     /* HBM admission budget (0 -> 150 GiB) */
+    int64_t max_particles;    /* particles in flight (0 -> no cap); a lone request is always admitted */
+    int32_t policy;           /* TFG_SERVER_LEAST_WORK or TFG_SERVER_FIFO */
+    int32_t discard_results;  /* 1: do not download finished simulations (throughput runs) */
+} tfg_server_desc;
+
+typedef struct tfg_server_stats {
+    int64_t submitted, completed, failed;
+    int64_t queued, running;          /* now */
+    int64_t particles_in_flight, bytes_in_flight;
+    int64_t max_concurrent;           /* largest number of simulations in flight so far */
+    int64_t chunks;                   /* chunks launched over all batches */
+} tfg_server_stats;
+
+TFG_API int tfg_server_create(const tfg_server_desc *desc, tfg_server **out);
+TFG_API int tfg_server_destroy(tfg_server *srv);
+/* A request for one simulation of `nsteps` steps; the engine description is a batch
+ * member's (tfg_batch_add_sim).  Calls on the request record the model host-side. */
+TFG_API int tfg_request_create(const tfg_engine_desc *desc, int max_type, int nr_species, int nsteps,
+                               tfg_request **out);
+TFG_API int tfg_request_free(tfg_request *req);
+TFG_API int tfg_request_set_type(tfg_request *req, int type, int dynamics, float mass);
+TFG_API int tfg_request_set_potential(tfg_request *req, int ti, int tj, const tfg_potential *p);
+TFG_API int tfg_request_add_flux(tfg_request *req, int ti, int tj, const tfg_flux *flux);
+TFG_API int tfg_request_set_species_flags(tfg_request *req, int nr, const uint32_t *flags);
+TFG_API int tfg_request_set_random_force(tfg_request *req, int type, float mean, float std, int duration_steps);
+TFG_API int tfg_request_set_boundary(tfg_request *req, int wall, const tfg_boundary *bc);
+TFG_API int tfg_request_set_boundary_potential(tfg_request *req, int wall, int type, const tfg_potential *p);
+TFG_API int tfg_request_set_bonded_potential(tfg_request *req, int slot, const tfg_potential *p);
+TFG_API int tfg_request_load_particles(tfg_request *req, int n, const float *x, const float *v, const int32_t *type,
+                                       const float *radius, const float *imass, const uint32_t *flags,
+                                       const float *species, const float *force_i);
+TFG_API int tfg_request_load_bonds(tfg_request *req, int n, const int32_t *i, const int32_t *j, const int32_t *slot);
+TFG_API int tfg_request_load_angles(tfg_request *req, int n, const int32_t *i, const int32_t *j, const int32_t *k,
+                                    const int32_t *slot);
+/* Submit (arrival = now); the server takes the request over (do not free it).  *id names
+ * the request from now on.  A request larger than the whole budget is refused. */
+TFG_API int tfg_server_submit(tfg_server *srv, tfg_request *req, int64_t *id);
+/* One turn of the serving loop: admit, launch chunks on idle batches, retire finished
+ * chunks.  If nothing finished, waits up to wait_us microseconds for a chunk to finish.
+ * *completed (may be NULL) = requests finished or failed during this call. */
+TFG_API int tfg_server_poll(tfg_server *srv, int wait_us, int *completed);
+/* Ids of the requests finished or failed since the last call, up to cap; *n = how many. */
+TFG_API int tfg_server_take_finished(tfg_server *srv, int64_t *ids, int cap, int *n);
+/* State (TFG_REQ_*) and status (TFG_OK or the failure) of a request; times in seconds on
+ * the server's clock (steady clock since creation): submitted, admitted, finished (-1 if
+ * not yet).  Any pointer may be NULL. */
+TFG_API int tfg_server_request_info(tfg_server *srv, int64_t id, int *state, int *status, double times[3]);
+/* Result of a finished request: particle count, then positions (n*3, global), velocities
+ * (n*3), species (n*nr_species) in id order and the FP64 totals.  Pass NULL arrays to read
+ * n first.  tfg_server_release forgets a finished request. */
+TFG_API int tfg_server_result(tfg_server *srv, int64_t id, int *n, float *x, float *v, float *species,
+                              tfg_reductions *red);
+TFG_API int tfg_server_release(tfg_server *srv, int64_t id);
+TFG_API int tfg_server_get_stats(tfg_server *srv, tfg_server_stats *out);
+TFG_API const char *tfg_server_last_error(const tfg_server *srv);
 
 /* Measured FP32 FMA throughput of `device` in TFLOP/s (2 flops per FMA), from a
  * register-only kernel with eight independent FMA chains per thread.  Measurement

@@ -18,8 +18,8 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["csrc/tfg_engine.cu", "csrc/tfg_api.cu", "csrc/tfg_kernels.cu", "csrc/tfg_pair.cu",
-              "csrc/tfg_pair_tile.cu", "csrc/tfg_probe.cu", "csrc/tfg_noalloc.cu"]
-CXX_SOURCES = ["host/tfg_potential.cpp"]
+              "csrc/tfg_pair_tile.cu", "csrc/tfg_pair_home.cu", "csrc/tfg_probe.cu", "csrc/tfg_noalloc.cu"]
+CXX_SOURCES = ["host/tfg_potential.cpp", "host/tfg_server.cpp"]
 HEADERS = ["csrc/tfg_device.cuh", "csrc/tfg_internal.h", "csrc/tfg_kernels.h", "csrc/tfg_engine_impl.h"]
 
 

@@ -43,12 +43,13 @@ int make_engine(int device, int max_type, int nspec, tfg_engine **out) {
     for (auto &p : eng->h_bpots) std::memset(&p, 0, sizeof(p));
     eng->h_btables.assign(kMaxBondSlots, std::vector<float>());
     int rc;
-    if ((rc = dalloc(eng, &eng->err, 1)) || (rc = dalloc(eng, &eng->overflow_count, 2)) ||
+    if ((rc = dalloc(eng, &eng->err, 2)) || (rc = dalloc(eng, &eng->overflow_count, 2)) ||
         (rc = dalloc(eng, &eng->bpots, kMaxBondSlots)) || (rc = dalloc(eng, &eng->stamps, 5))) {
         destroy(eng);
         return rc;
     }
-    cudaMemset(eng->err, 0, sizeof(uint32_t));
+    eng->err_slots = 1;
+    cudaMemset(eng->err, 0, 2 * sizeof(uint32_t));
     cudaMemset(eng->overflow_count, 0, 2 * sizeof(int));
     cudaMemset(eng->stamps, 0, sizeof(unsigned long long) * 5);
     if (cudaDeviceSynchronize() != cudaSuccess) {
@@ -355,7 +356,8 @@ TFG_API int tfg_autotune(tfg_engine *eng, int *split) {
 }
 
 TFG_API int tfg_set_split(tfg_engine *eng, int split) {
-    if (!eng || !(split == 1 || split == 2 || split == 7 || split == 14)) return TFG_E_INVAL;
+    if (!eng || !(split == 1 || split == 2 || split == 7 || split == 14 || split == TFG_PAIR_HOME_OUTER))
+        return TFG_E_INVAL;
     eng->split = split;
     eng->gen++;
     return TFG_OK;
@@ -485,6 +487,11 @@ TFG_API int tfg_get_verlet(tfg_engine *eng, int64_t *rebuilds, float *maxdx) {
     if (!eng) return TFG_E_INVAL;
     return verlet_sim(eng, 0, rebuilds, maxdx);
 }
+TFG_API int tfg_batch_sim_status(tfg_engine *eng, int sim, int *status) {
+    if (!eng) return TFG_E_INVAL;
+    return sim_status(eng, sim, status);
+}
+
 TFG_API int tfg_batch_get_verlet(tfg_engine *eng, int sim, int64_t *rebuilds, float *maxdx) {
     if (!eng) return TFG_E_INVAL;
     return verlet_sim(eng, sim, rebuilds, maxdx);

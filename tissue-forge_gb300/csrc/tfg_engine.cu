@@ -125,6 +125,8 @@ template <typename T> int ensure(tfg_engine *eng, T **p, size_t &cap, size_t nee
 int relayout(tfg_engine *eng) {
     cudaStream_t s = eng->stream;
     const int T = eng->max_type;
+    // errors raised under the old layout belong to the simulations of the old order
+    if (int rc0 = collect_errors(eng)) return rc0;
     std::vector<int> order;
     for (int k = 0; k < (int)eng->sims.size(); k++)
         if (eng->sims[k].live && eng->sims[k].loaded) order.push_back(k);
@@ -245,6 +247,12 @@ int relayout(tfg_engine *eng) {
         eng->cells_cap = cc;
     }
     CK(cudaMemcpyAsync(eng->cell_sim, cell_sim.data(), sizeof(int32_t) * std::max(C, 1), cudaMemcpyHostToDevice, s));
+    if ((int)order.size() > eng->err_slots) {
+        const int slots = std::max((int)order.size(), 2 * eng->err_slots);
+        if ((rc = dalloc(eng, &eng->err, 1 + (size_t)slots))) return rc;
+        eng->err_slots = slots;
+    }
+    CK(cudaMemsetAsync(eng->err, 0, sizeof(uint32_t) * (1 + (size_t)eng->err_slots), s));
     size_t rneed = std::max<size_t>(order.size(), 1) * RED_COUNT;
     if ((rc = ensure(eng, &eng->red, eng->red_cap, rneed))) return rc;
     CK(cudaMemsetAsync(eng->red, 0, sizeof(double) * rneed, s));
@@ -418,18 +426,60 @@ int check_launch(tfg_engine *eng) {
     return TFG_OK;
 }
 
-int read_err(tfg_engine *eng) {
-    uint32_t flags = 0;
-    CK(cudaMemcpyAsync(&flags, eng->err, sizeof(uint32_t), cudaMemcpyDeviceToHost, eng->stream));
+static int err_code(uint32_t flags) {
+    if (flags & ERR_NAN) return TFG_E_NAN;
+    if (flags & ERR_RANGE) return TFG_E_RANGE;
+    if (flags & ERR_TOOFAST) return TFG_E_TOOFAST;
+    if (flags & ERR_OVERFLOW) return TFG_E_OVERFLOW;
+    return TFG_OK;
+}
+
+// Read and clear the device error words.  A simulation's word goes to its sticky status
+// (the reference flags the offending particle, toofast_error, tf_engine_advance.cpp:72-85,
+// 204-206; here the simulation is the unit that fails), the engine's word to pending_err.
+int collect_errors(tfg_engine *eng) {
+    const int ns = std::min((int)eng->order.size(), eng->err_slots);
+    std::vector<uint32_t> w(1 + ns, 0u);
+    CK(cudaMemcpyAsync(w.data(), eng->err, sizeof(uint32_t) * (1 + ns), cudaMemcpyDeviceToHost, eng->stream));
     CK(cudaStreamSynchronize(eng->stream));
+    bool any = false;
+    for (uint32_t x : w) any |= x != 0u;
+    if (!any) return TFG_OK;
+    CK(cudaMemsetAsync(eng->err, 0, sizeof(uint32_t) * (1 + ns), eng->stream));
+    CK(cudaStreamSynchronize(eng->stream));
+    eng->pending_err |= w[0];
+    for (int q = 0; q < ns; q++) {
+        SimHost &S = eng->sims[eng->order[q]];
+        if (w[1 + q] && S.status == TFG_OK) S.status = err_code(w[1 + q]);
+    }
+    return TFG_OK;
+}
+
+int read_err(tfg_engine *eng) {
+    int rc = collect_errors(eng);
+    if (rc) return rc;
+    const uint32_t flags = eng->pending_err;
+    eng->pending_err = 0u;
     if (flags) {
-        CK(cudaMemsetAsync(eng->err, 0, sizeof(uint32_t), eng->stream));
-        CK(cudaStreamSynchronize(eng->stream));
-        if (flags & ERR_NAN) return fail(eng, TFG_E_NAN, "non-finite particle position");
-        if (flags & ERR_RANGE) return fail(eng, TFG_E_RANGE, "particle outside the space");
-        if (flags & ERR_TOOFAST) return fail(eng, TFG_E_TOOFAST, "particle moved more than one cell in a step");
+        std::string which;
+        for (int k : eng->order)
+            if (eng->sims[k].status != TFG_OK) which += (which.empty() ? " (simulation " : ", ") + std::to_string(k);
+        if (!which.empty()) which += ")";
+        if (flags & ERR_NAN) return fail(eng, TFG_E_NAN, "non-finite particle position" + which);
+        if (flags & ERR_RANGE) return fail(eng, TFG_E_RANGE, "particle outside the space" + which);
+        if (flags & ERR_TOOFAST)
+            return fail(eng, TFG_E_TOOFAST, "particle moved more than one cell in a step" + which);
         if (flags & ERR_OVERFLOW) return fail(eng, TFG_E_OVERFLOW, "capacity exceeded");
     }
+    return TFG_OK;
+}
+
+int sim_status(tfg_engine *eng, int sim, int *status) {
+    int rc = sim_check(eng, sim);
+    if (rc) return rc;
+    if (!status) return TFG_E_INVAL;
+    if ((rc = collect_errors(eng))) return rc;
+    *status = eng->sims[sim].status;
     return TFG_OK;
 }
 
@@ -977,10 +1027,11 @@ int autotune(tfg_engine *eng) {
     int rc = dalloc(eng, &save, nq);
     if (rc) return rc;
     CK(cudaMemcpyAsync(save, eng->A[eng->cur].sq, sizeof(float) * nq, cudaMemcpyDeviceToDevice, s));
-    const int cand[4] = {1, 2, 7, 14};
+    const int cand[5] = {1, 2, 7, 14, TFG_PAIR_HOME_OUTER};
+    const int ncand = pair_home_eligible(pair_args(eng)) ? 5 : 4;
     float best = 1e30f;
     int best_split = 1;
-    for (int c = 0; c < 4; c++) {
+    for (int c = 0; c < ncand; c++) {
         float tmin = 1e30f;
         for (int rep = 0; rep < 3; rep++) {
             rc = bin(eng, 0);

@@ -45,6 +45,7 @@ struct SimHost {
     tfg_boundary walls[6];           // as set (NO_SLIP already turned into VELOCITY)
     std::vector<tfg::PotDev> wpots;  // 6 x max_type wall potentials
     std::vector<std::vector<float>> wtables;
+    int status = 0;                  // first error of this simulation (TFG_E_*), sticky
 };
 
 struct tfg_engine {
@@ -101,7 +102,11 @@ struct tfg_engine {
     std::vector<std::vector<float>> h_btables;
     double *red = nullptr;
     size_t red_cap = 0;
+    // device error words: err[0] for the engine, err[1 + q] for the simulation at arena
+    // slot q (order[q]); collected into SimHost::status and pending_err at every read
     uint32_t *err = nullptr;
+    int err_slots = 0;               // simulation words allocated after err[0]
+    uint32_t pending_err = 0;        // engine bits collected but not yet reported
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaEvent_t ev[5] = {};          // autotuner timing
@@ -147,6 +152,8 @@ template <typename T> int dalloc(tfg_engine *eng, T **p, size_t count) {
 }
 int check_launch(tfg_engine *eng);
 int read_err(tfg_engine *eng);
+int collect_errors(tfg_engine *eng);            // device error words -> SimHost::status, pending_err
+int sim_status(tfg_engine *eng, int sim, int *status);
 int sim_check(tfg_engine *eng, int sim);        // TFG_OK when `sim` names a live simulation
 int add_sim(tfg_engine *eng, const tfg_engine_desc *d, int *out);
 int commit(tfg_engine *eng);                    // re-lay the arena out and upload tables when dirty

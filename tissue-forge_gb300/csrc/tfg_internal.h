@@ -101,6 +101,17 @@ struct TilePlan {
 TilePlan plan_pair_tile(int nsims, int max_type, int blob_floats);
 void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overflow_list, int *overflow_count, int sms,
                       bool signature, int split, cudaStream_t s);
+// Overflow pass of the tiled kernels' table variant: the home cells listed in
+// overflow_list[0 .. overflow_count[0]), one warp each, global-memory candidates and atomics.
+void launch_pair_overflow(const PairKernelArgs &a, int *overflow_list, int *overflow_count, bool signature, int sms,
+                          cudaStream_t s);
+// Home-particle-outer pass (split TFG_PAIR_HOME_OUTER): tabulated potentials only, no DPD,
+// fluxes or Verlet pair lists.  overflow_count must be zeroed before the launch.
+void launch_pair_home(const PairKernelArgs &a, int *overflow_list, int *overflow_count, int sms, bool signature,
+                      cudaStream_t s);
+inline bool pair_home_eligible(const PairKernelArgs &a) {
+    return !a.has_dpd && !(a.nspec > 0 && a.has_flux) && !a.vlist && a.flux_sub < 0;
+}
 int pair_tile_capacity();
 void launch_pair_stencil_fluxonly(const PairKernelArgs &a, cudaStream_t s);
 // Flux-only substep pass (a.flux_sub >= 0): species flux increments of the pair set, no

@@ -142,6 +142,7 @@ __global__ void k_setpartp(int n, const float *__restrict__ xg, SimParams P, flo
         ind[k] = (int)__fmul_rn(__fsub_rn(x[k], o3[k]), i3[k]);
         if (ind[k] < 0 || ind[k] >= P.cdim[k]) {
             atomicOr(err, ERR_RANGE);
+            atomicOr(err + 1 + P.red_base / RED_COUNT, ERR_RANGE);
             ind[k] = ind[k] < 0 ? 0 : P.cdim[k] - 1;
         }
     }
@@ -515,7 +516,10 @@ __global__ void k_advance(int n, int cap, int nspec, SimParams *sims, const int3
         bool migrated = false;
         if (P.flags & TFG_ENGINE_VERLET) {
             const float d2 = advance_verlet(P, type_dyn[P.type_base + type] == TFG_NEWTONIAN, f, imass, p, v, oldx[i]);
-            if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(err, ERR_NAN);
+            if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) {
+                atomicOr(err, ERR_NAN);
+                atomicOr(err + 1 + rb / RED_COUNT, ERR_NAN);
+            }
             pos[i] = p;
             vel[i] = v;
             vsim = cell_sim[c0];
@@ -583,7 +587,11 @@ __global__ void k_advance(int n, int cap, int nspec, SimParams *sims, const int3
             }
             if (delta[0] | delta[1] | delta[2]) {
                 for (int k = 0; k < 3; k++) {
-                    if (x[k] >= P.h2[k] || x[k] <= -P.h[k]) { atomicOr(err, ERR_TOOFAST); break; }
+                    if (x[k] >= P.h2[k] || x[k] <= -P.h[k]) {
+                        atomicOr(err, ERR_TOOFAST);
+                        atomicOr(err + 1 + rb / RED_COUNT, ERR_TOOFAST);
+                        break;
+                    }
                     x[k] = __fadd_rn(x[k], -__fmul_rn((float)delta[k], P.h[k]));
                 }
                 int a, b, c;
@@ -593,7 +601,10 @@ __global__ void k_advance(int n, int cap, int nspec, SimParams *sims, const int3
                 migrated = true;
                 mig = 1.f;
             }
-            if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) atomicOr(err, ERR_NAN);
+            if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) {
+                atomicOr(err, ERR_NAN);
+                atomicOr(err + 1 + rb / RED_COUNT, ERR_NAN);
+            }
             pos[i] = make_float4(x[0], x[1], x[2], p.w);
             vel[i] = make_float4(vv[0], vv[1], vv[2], inv_nd);
         }

@@ -831,6 +831,20 @@ void launch_variant(const TileArgs &T0, cudaStream_t s, int sms) {
 
 int pair_tile_capacity() { return kCapT; }
 
+void launch_pair_overflow(const PairKernelArgs &a, int *overflow_list, int *overflow_count, bool signature, int sms,
+                          cudaStream_t s) {
+    TileArgs T;
+    T.a = a;
+    T.overflow_list = overflow_list;
+    T.overflow_count = overflow_count;
+    T.split = 1;
+    T.stage_floats = 0;
+    T.stage_pots = 0;
+    if (signature) k_pair_overflow<false, false, false, true><<<sms, 256, 0, s>>>(T);
+    else if (!(a.flags & TFG_ENGINE_NO_DENSITY)) k_pair_overflow<false, false, true, false><<<sms, 256, 0, s>>>(T);
+    else k_pair_overflow<false, false, false, false><<<sms, 256, 0, s>>>(T);
+}
+
 void launch_pair_fluxonly(const PairKernelArgs &a, const TilePlan &plan, int *overflow_list, int *overflow_count,
                           int sms, bool tile, cudaStream_t s) {
     if (!tile) {
@@ -871,6 +885,10 @@ void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overfl
     if (a.n <= 0) return;
     const bool dpd = a.has_dpd, flux = a.nspec > 0 && a.has_flux;
     const bool dens = !(a.flags & TFG_ENGINE_NO_DENSITY);
+    if (split == TFG_PAIR_HOME_OUTER && pair_home_eligible(a)) {
+        launch_pair_home(a, overflow_list, overflow_count, sms, signature, s);
+        return;
+    }
     if (signature) {
         if (a.vlist) launch_variant<false, false, false, true, true>(T, s, sms);
         else launch_variant<false, false, false, true>(T, s, sms);

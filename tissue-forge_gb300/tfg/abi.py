@@ -31,6 +31,8 @@ POTENTIAL_HARMONIC = 1 << 7
 POTENTIAL_SCALED = 1 << 11
 POTENTIAL_SHIFTED = 1 << 12
 POTENTIAL_CHUNK = 8
+# tfg_set_split / tfg_autotune: the home-particle-outer pair kernel (tabulated potentials only)
+PAIR_HOME_OUTER = 32
 
 FLUX_FICK = 0
 FLUX_SECRETE = 1
