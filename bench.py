@@ -220,17 +220,11 @@ def fp32_peak(dev):
     return peak.value
 
 
-def profiled_traffic(name, pairs):
-    """DRAM bytes of one pair-kernel launch from the committed ncu summary profiles/<name>
-    (dram__bytes_read.sum + dram__bytes_write.sum of one captured launch), scaled to `pairs`."""
-    try:
-        vals = {}
-        for line in open(os.path.join(ROOT, "profiles", name)):
-            if ":" in line and line.split(":")[0] in ("traffic_bytes_per_launch", "pairs_per_launch"):
-                vals[line.split(":")[0]] = float(line.split(":")[1])
-        return vals["traffic_bytes_per_launch"] * pairs / vals["pairs_per_launch"]
-    except Exception:
-        return None
+# DRAM traffic of the tiled pair kernel per particle of the arena: one ncu capture of the
+# 256-simulation ensemble pass (2,902,298 particles) read 130.9 MB and wrote 20.8 MB
+# (dram__bytes_read.sum + dram__bytes_write.sum), 52.3 B per particle.  The traffic is the
+# particle data read and the forces written, so it scales with the particles, not the pairs.
+PAIR_TRAFFIC_BYTES_PER_PARTICLE = 52.3
 
 
 def launches_per_step(has_bonds=False, has_angles=False):
@@ -271,18 +265,20 @@ def cpu_rate_sims(ws, threads, budget_s, max_steps=50):
     return tot_ps / tot_t, steps_done, tot_t
 
 
-def run_reference(args, rank, world):
-    if rank != 0:
-        return
-    threads = os.cpu_count() or 1
-    if args.workload in ("ensemble", "served"):
-        from tfg import configs
-        ws = ensemble_sample(configs.ensemble(count=args.sims, seed=0), 16)
-        sample = ("16 of the 256 simulations (every 16th, %d particles) advanced one engine step each per "
-                  "timed step, threaded oracle" % sum(w.n for w in ws))
-    else:
-        ws = [make_workload(args.workload, 0, args.n or None, args.relax)]
-        sample = "one engine step of the %s workload per timed step, threaded oracle" % args.workload
+CPU_SAMPLE_SIMS = 16     # simulations of the ensemble in the bounded CPU sample
+CPU_SAMPLE_ROUNDS = 12   # timed rounds; each round steps every sampled simulation once
+
+
+def ensemble_cpu_sample(sims):
+    """The bounded CPU sample of the ensemble, the same for the reference arm and the GPU
+    line's cpu_baseline: every (sims/16)-th simulation of the ensemble in its natural order."""
+    from tfg import configs
+    return ensemble_sample(configs.ensemble(count=sims), CPU_SAMPLE_SIMS)
+
+
+def cpu_rate_rounds(ws, threads, rounds, warmup):
+    """Particle-steps/s of the CPU restatement (threaded, as the reference's runners) over
+    `rounds` rounds in which every simulation of `ws` takes one engine step."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from tfg.engine import setup_model
@@ -290,27 +286,56 @@ def run_reference(args, rank, world):
     for w in ws:
         e = O.OracleEngine(w.desc(), 0, threads, signature=False)
         engines.append((e, setup_model(e, w), w.n))
-    for k in range(args.warmup):
+    for _ in range(warmup):
         for e, _, _ in engines:
             e.step(1)
     ps, t = 0.0, 0.0
-    steps = min(args.steps, 30)
-    for k in range(steps):
+    for _ in range(rounds):
         t0 = time.perf_counter()
         for e, _, n in engines:
             e.step(1)
             ps += n
         t += time.perf_counter() - t0
-    value = ps / t
+    return ps / t, t
+
+
+def ensemble_config(sims, world, n_all):
+    """`config` of the ensemble line: the workload only (sims per rank, the whole job's
+    simulations and particles), the same in both arms."""
+    return {"workload": "ensemble", "description": WORKLOADS["ensemble"]["desc"], "sims_per_rank": sims,
+            "sims_all_ranks": sims * world, "n_particles_all_ranks": n_all,
+            "l2": "working set larger than L2 (not flushed)", "parallelism": "replicas%d" % world}
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU engine on the host cores: the CPU restatement (the reference
+    itself cannot be built here), threaded like the reference's runners, on a bounded sample
+    of the GPU line's workload, with the GPU line's config, metric and unit."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    if args.workload in ("ensemble", "served"):
+        from tfg import configs
+        ws = ensemble_cpu_sample(args.sims)
+        ns, _ = configs.ensemble_sizes(args.sims * world)
+        config = ensemble_config(args.sims, world, int(np.sum(ns)))
+        rounds = CPU_SAMPLE_ROUNDS
+        sample = ("%d of the %d simulations (every %dth, %d particles), %d rounds of one engine step each, "
+                  "threaded CPU restatement of the reference engine" % (
+                      len(ws), args.sims, max(1, args.sims // CPU_SAMPLE_SIMS), sum(w.n for w in ws), rounds))
+    else:
+        ws = [make_workload(args.workload, 0, args.n or None, args.relax)]
+        config = {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"], "n_particles": ws[0].n}
+        rounds = min(args.steps, 30)
+        sample = "%d engine steps of the %s workload, threaded CPU restatement" % (rounds, args.workload)
+    value, t = cpu_rate_rounds(ws, threads, rounds, args.warmup)
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
-        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / steps,
+        "steps": rounds, "warmup": args.warmup, "ms_per_step": 1e3 * t / rounds,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "impl": "reference",
-        "config": {"workload": args.workload, "description": WORKLOADS[args.workload]["desc"],
-                   "n_particles_sampled": sum(w.n for w in ws)},
+        "impl": "reference", "config": config,
         "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-                         "sample": sample + " (CPU restatement of the reference engine)"},
+                         "sample": sample},
         "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -364,6 +389,7 @@ def run_ensemble(args, rank, world, dev, dist):
 
     b, sims = make_batch()
     split = b.autotune()
+    tuning = b.tuning()
     b.step(args.warmup)
     cnt0, _ = b.pair_signature()
     pairs0 = int(cnt0.sum()) // 2
@@ -457,14 +483,14 @@ def run_ensemble(args, rank, world, dev, dist):
     peak = fp32_peak(dev)
     hbm, hbm_src = hbm_peak()
     bytes_alg = n_tot * WORKLOADS["ensemble"]["bytes_per_particle"]
-    roof = {"bound": "fp32", "kernel": "k_pair_tile (split %d)" % split, "achieved": achieved, "peak": peak,
+    roof = {"bound": "fp32", "kernel": pair_kernel_name(split), "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
             "peak_source": "measured live (tfg_probe_fp32_tflops, FFMA chains)",
             "flops_per_launch": fl_pair, "pairs_per_step": pairs,
             "flops_per_pair": FLOPS["table"] + FLOPS["density"], "kernel_ms": phase[1],
-            "traffic": profiled_traffic("k_pair_tile_ensemble256_traffic.md", pairs),
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
-                              "(profiles/k_pair_tile_ensemble256_traffic.md), scaled by pairs",
+            "traffic": PAIR_TRAFFIC_BYTES_PER_PARTICLE * n_tot,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of the tiled "
+                              "kernel on this ensemble (52.3 B per particle), scaled by the particles",
             "algorithmic_bytes_per_launch": n_tot * 56,
             "step_hbm": {"achieved_gbs": bytes_alg / (step_ms * 1e-3) / 1e9, "peak_gbs": hbm,
                          "peak_source": hbm_src, "frac": bytes_alg / (step_ms * 1e-3) / 1e9 / hbm,
@@ -472,13 +498,19 @@ def run_ensemble(args, rank, world, dev, dist):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
+        # the same sample and timing as bench.py --impl reference
         threads = os.cpu_count() or 1
-        sample = ensemble_sample(ws, 16)
-        rate, steps, dt = cpu_rate_sims(sample, threads, 15.0, max_steps=40)
+        sample = ensemble_cpu_sample(args.sims)
+        rate, dt = cpu_rate_rounds(sample, threads, CPU_SAMPLE_ROUNDS, args.warmup)
         cpu = {"value": rate, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-               "sample": "16 of the %d simulations (every %dth, %d particles), %d-%d steps each on the threaded "
-                         "CPU restatement of the reference engine, %.1f s" % (
-                             len(ws), max(1, len(ws) // 16), sum(w.n for w in sample), min(steps), max(steps), dt)}
+               "sample": "%d of the %d simulations (every %dth, %d particles), %d rounds of one engine step each, "
+                         "threaded CPU restatement of the reference engine, %.1f s" % (
+                             len(sample), args.sims, max(1, args.sims // CPU_SAMPLE_SIMS), sum(w.n for w in sample),
+                             CPU_SAMPLE_ROUNDS, dt)}
+    workloads = None
+    if rank == 0 and args.sub_workloads:
+        workloads = {name: measure_workload(name, dev, stream, args.sub_steps, args.warmup)
+                     for name in args.sub_workloads.split(",")}
     serving = serve_sample(args, dev, args.requests) if (rank == 0 and args.requests > 0) else None
     if serving is not None and args.sustained_requests > 0:
         # the same stream at an arrival rate the GPU sustains (about half its served capacity),
@@ -495,17 +527,65 @@ def run_ensemble(args, rank, world, dev, dist):
             "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "ensemble", "description": WORKLOADS["ensemble"]["desc"], "sims": len(ws),
-                       "n_particles": n_tot, "sims_all_ranks": args.sims * world, "n_particles_all_ranks": n_all,
-                       "sharding": "LPT over ranks by particle count, no data-path collective", "l2": "working set larger than L2 (not flushed)",
-                       "parallelism": "replicas%d" % world, "pair_split": split, "graphs": True,
-                       "phase_ms_per_step": dict(zip(["bin", "pair", "bonded", "advance"], phase.round(5).tolist()))},
+            "config": ensemble_config(args.sims, world, n_all),
+            "details": {"sharding": "LPT over ranks by particle count, no data-path collective",
+                        "sims_this_rank": len(ws), "n_particles_this_rank": n_tot,
+                        "pair_split": split, "pair_kernel": pair_kernel_name(split), "graphs": True,
+                        "pair_tuning": dict(zip(["split", "warps_per_cta", "grab"], tuning)),
+                        "phase_ms_per_step": dict(zip(["bin", "pair", "bonded", "advance"], phase.round(5).tolist()))},
             "plain_gpu": plain, "batched_over_plain": value / plain["value"],
-            "serving": serving,
+            "serving": serving, "workloads": workloads,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk.summary(),
             "gpu_launches": launches_per_step() * args.steps,
         }
         print(json.dumps(line), flush=True)
+
+
+def pair_kernel_name(split):
+    return "k_pair_home" if split == 32 else "k_pair_tile (split %d)" % split
+
+
+def measure_workload(name, dev, stream, steps, warmup):
+    """One single-simulation workload at its configured size on the plain path: particle-
+    steps/s over `steps` steps with the L2 flushed before each, the pair kernel's time from
+    stamped steps, and its FP32 roofline fraction (algorithmic flops of the interacting pairs)."""
+    import torch
+    from tfg.engine import Engine, setup_model
+    w = make_workload(name, 0)
+    eng = Engine(w.desc(device=dev))
+    keep = setup_model(eng, w)
+    eng.set_stream(stream.cuda_stream)
+    if w.relax_steps:
+        for t in range(w.max_type):
+            eng.set_type(t, 1, w.mass[t])
+        eng.step(w.relax_steps)
+        for t in range(w.max_type):
+            eng.set_type(t, w.dynamics[t], w.mass[t])
+    split = eng.autotune()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    value = timed_rate(eng, w.n, steps, warmup, flush, stream)
+    cnt, _ = eng.pair_signature()
+    pairs = int(cnt.sum()) // 2
+    eng.set_phase_timing(True)
+    eng.step(2)
+    ph = np.zeros(4)
+    for _ in range(5):
+        flush.zero_()
+        eng.step(1)
+        ph += np.array(eng.phase_ms())
+    ph /= 5
+    fl = pairs * pair_flops(w)
+    peak = fp32_peak(dev)
+    achieved = fl / (ph[1] * 1e-3) / 1e12
+    del eng, keep
+    return {"value": value, "unit": "particle-steps/s", "n_particles": w.n, "steps": steps,
+            "ms_per_step": w.n * 1e3 / value, "description": WORKLOADS[name]["desc"],
+            "l2": "flushed between timed steps (256 MiB write)",
+            "roofline": {"bound": "fp32", "kernel": pair_kernel_name(split), "kernel_ms": float(ph[1]),
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak else None, "pairs_per_step": pairs,
+                         "flops_per_pair": pair_flops(w)},
+            "phase_ms_per_step": dict(zip(["bin", "pair", "bonded", "advance"], ph.round(5).tolist()))}
 
 
 def run_served(args, rank, world, dev, dist):
@@ -611,7 +691,7 @@ def run_single(args, rank, world, dev, dist):
     step_ms = t_ms / args.steps
     bytes_alg = w.n * WORKLOADS[args.workload]["bytes_per_particle"]
     hbm, hbm_src = hbm_peak()
-    roof = {"bound": "fp32", "kernel": "k_pair_tile (split %d)" % split, "achieved": achieved, "peak": peak,
+    roof = {"bound": "fp32", "kernel": pair_kernel_name(split), "achieved": achieved, "peak": peak,
             "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
             "peak_source": "measured live (tfg_probe_fp32_tflops, FFMA chains)",
             "flops_per_launch": fl_pair, "pairs_per_step": pairs, "flops_per_pair": pair_flops(w),
@@ -683,6 +763,9 @@ def main():
     ap.add_argument("--serve-particles", type=int, default=2_000_000, help="particles in flight cap")
     ap.add_argument("--quantum", type=int, default=50, help="largest chunk of steps between admissions")
     ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--sub-workloads", default="bonded_fluid,dpd_droplets",
+                    help="single-simulation workloads measured beside the ensemble (comma list; empty: none)")
+    ap.add_argument("--sub-steps", type=int, default=40, help="timed steps of each of those workloads")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 

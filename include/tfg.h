@@ -183,8 +183,9 @@ typedef struct tfg_engine_desc {
 /* ---- boundary conditions (BoundaryConditions, tfBoundaryConditions.h:39-261) ----
  * Walls: 0 left (x low), 1 right (x high), 2 front (y low), 3 back (y high), 4 bottom
  * (z low), 5 top (z high).  Every wall starts PERIODIC.  An axis is periodic when both its
- * walls are; a PERIODIC wall facing a non-periodic one makes both periodic
- * (check_periodicy, tfBoundaryConditions.cpp:192-216).  On a non-periodic axis no cell pair
+ * walls are; a PERIODIC wall facing a non-periodic one makes both exactly PERIODIC
+ * (check_periodicy, tfBoundaryConditions.cpp:192-216), while two PERIODIC walls keep their
+ * other bits (RESETTING).  On a non-periodic axis no cell pair
  * crosses the box edge (space_init task list, tfSpace.cpp:905-1000).  Walls with FREESLIP or
  * VELOCITY reflect particles that cross them (apply_update_pos_vel,
  * tf_boundary_eval.h:46-134); NO_SLIP is VELOCITY with zero velocity
@@ -196,6 +197,13 @@ typedef struct tfg_engine_desc {
 #define TFG_BOUNDARY_FREESLIP  (1u << 2)
 #define TFG_BOUNDARY_POTENTIAL (1u << 3)
 #define TFG_BOUNDARY_NO_SLIP   (1u << 4)
+/* BOUNDARY_RESETTING (tfBoundaryConditions.h:44): with PERIODIC on both walls of an axis, a
+ * particle that wraps around the box through this wall (moves into a cell on this wall from
+ * the cell on the opposite wall) has its species values reset to the simulation's reset
+ * values (StateVector::reset, state/tfStateVector.cpp:36-44: each species' initial
+ * concentration, 0 when unset; tfg_set_species_reset); apply_boundary_particle_crossing,
+ * tfBoundaryConditions.cpp:676-735, called at migration, tf_engine_advance.cpp:219. */
+#define TFG_BOUNDARY_RESETTING (1u << 5)
 
 typedef struct tfg_boundary {
     uint32_t kind;         /* TFG_BOUNDARY_* */
@@ -234,6 +242,9 @@ TFG_API int tfg_set_potential(tfg_engine *eng, int ti, int tj, const tfg_potenti
 TFG_API int tfg_add_flux(tfg_engine *eng, int ti, int tj, const tfg_flux *flux);
 /* Species flags per species index: bit0 = SPECIES_KONSTANT (tfFlux.cpp:177-179). */
 TFG_API int tfg_set_species_flags(tfg_engine *eng, int nr, const uint32_t *flags);
+/* Species values a particle takes when it crosses a RESETTING boundary: nr values, one per
+ * species index (default 0). */
+TFG_API int tfg_set_species_reset(tfg_engine *eng, int nr, const float *values);
 /* Gaussian single-body force per type (Force::random, tfForce.cpp:111-245): redraw
  * when (time + id) % duration_steps == 0; std <= 0 disables. */
 TFG_API int tfg_set_random_force(tfg_engine *eng, int type, float mean, float std, int duration_steps);
@@ -291,6 +302,13 @@ TFG_API int tfg_set_pair_lists(tfg_engine *eng, int enable);
 #define TFG_PAIR_HOME_OUTER 32
 TFG_API int tfg_autotune(tfg_engine *eng, int *split);
 TFG_API int tfg_set_split(tfg_engine *eng, int split);
+/* The whole tuple the autotuner picks: the split (as above), the warps per CTA of the tiled
+ * kernel (8, or 4 for engines whose potentials are all tabulated: twice the CTAs per SM) and
+ * the home cells a warp takes from the shared work counter at a time (1..8; it times 1, 2, 4).
+ * The reference's counterparts are the hand-set blocks and threads of
+ * cuda::EngineConfig::setBlocks / setThreads (source/cuda/tfEngineConfig.cpp:98-124). */
+TFG_API int tfg_get_tuning(tfg_engine *eng, int *split, int *warps_per_cta, int *grab);
+TFG_API int tfg_set_tuning(tfg_engine *eng, int split, int warps_per_cta, int grab);
 /* Pair-set signature of the current binned state, per particle id: the number of
  * partners with r2 <= cutoff^2 and the wrap-around sum of a 32-bit mix of their ids.
  * It runs the pair pass's own stencil walk and pair decision (no forces).  Call it after
@@ -298,6 +316,12 @@ TFG_API int tfg_set_split(tfg_engine *eng, int split);
  * that did not rebuild at its last step is walked through its pair lists, as its next
  * force pass would be.  Verification hook; the reference has no counterpart. */
 TFG_API int tfg_pair_signature(tfg_engine *eng, int32_t *count, uint32_t *hash);
+/* The interacting pairs themselves, from the same kernels and pair decision as
+ * tfg_pair_signature: up to cap pairs (lower id, higher id), 2*cap ints, in no particular
+ * order; *count = all pairs found (cap 0: count only).  Ids are the arena's particle ids
+ * (for a single simulation, its particle ids).  Verification hook; no reference counterpart
+ * (the reference's pair set is the one its runner_dopair walk finds). */
+TFG_API int tfg_pair_list(tfg_engine *eng, int64_t cap, int32_t *pairs, int64_t *count);
 
 TFG_API int tfg_get_count(const tfg_engine *eng, int *n);
 /* Download per-particle state in id order.  Any pointer may be NULL.
@@ -347,6 +371,7 @@ TFG_API int tfg_batch_set_type(tfg_engine *eng, int sim, int type, int dynamics,
 TFG_API int tfg_batch_set_potential(tfg_engine *eng, int sim, int ti, int tj, const tfg_potential *p);
 TFG_API int tfg_batch_add_flux(tfg_engine *eng, int sim, int ti, int tj, const tfg_flux *flux);
 TFG_API int tfg_batch_set_species_flags(tfg_engine *eng, int sim, int nr, const uint32_t *flags);
+TFG_API int tfg_batch_set_species_reset(tfg_engine *eng, int sim, int nr, const float *values);
 TFG_API int tfg_batch_set_random_force(tfg_engine *eng, int sim, int type, float mean, float std,
                                        int duration_steps);
 TFG_API int tfg_batch_load_particles(tfg_engine *eng, int sim, int n, const float *x, const float *v,
@@ -365,6 +390,17 @@ TFG_API int tfg_batch_download(tfg_engine *eng, int sim, float *x, float *xrel, 
                                float *f, float *density, float *species, float *q);
 TFG_API int tfg_batch_get_reductions(tfg_engine *eng, int sim, tfg_reductions *out);
 TFG_API int tfg_batch_get_verlet(tfg_engine *eng, int sim, int64_t *rebuilds, float *maxdx);
+/* Resume a simulation saved mid-run: after tfg_batch_load_particles_binned (cells and
+ * cell-relative positions as tfg_download returns them), set its engine time (steps taken,
+ * the counter every random stream is keyed on) and, when q is not NULL, the flux increments
+ * its particles carry into the next step (n * nr_species in id order, tfg_download's q:
+ * particles that changed cell integrate theirs a step late, tf_engine_advance.cpp:222-236).
+ * The reference restores a saved Universe through FIO (tfSimulator.cpp:940-1020). */
+TFG_API int tfg_batch_resume(tfg_engine *eng, int sim, int64_t steps, const float *q);
+/* Deterministic pair pass (default off): the nonbonded forces are accumulated per particle
+ * in a fixed order (the stencil kernel, no atomics), so a run gives the same bits every
+ * time and a resumed run continues bit-identically.  Bonded forces still use atomics. */
+TFG_API int tfg_set_deterministic(tfg_engine *eng, int enable);
 /* Status of one simulation: TFG_OK, or the first error its particles raised (TFG_E_NAN,
  * TFG_E_TOOFAST, TFG_E_RANGE), kept until the simulation is removed.  The reference flags
  * the offending particle and fails the whole step (toofast_error,
@@ -429,6 +465,7 @@ TFG_API int tfg_request_set_type(tfg_request *req, int type, int dynamics, float
 TFG_API int tfg_request_set_potential(tfg_request *req, int ti, int tj, const tfg_potential *p);
 TFG_API int tfg_request_add_flux(tfg_request *req, int ti, int tj, const tfg_flux *flux);
 TFG_API int tfg_request_set_species_flags(tfg_request *req, int nr, const uint32_t *flags);
+TFG_API int tfg_request_set_species_reset(tfg_request *req, int nr, const float *values);
 TFG_API int tfg_request_set_random_force(tfg_request *req, int type, float mean, float std, int duration_steps);
 TFG_API int tfg_request_set_boundary(tfg_request *req, int wall, const tfg_boundary *bc);
 TFG_API int tfg_request_set_boundary_potential(tfg_request *req, int wall, int type, const tfg_potential *p);

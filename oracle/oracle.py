@@ -63,6 +63,7 @@ def lib():
         L.tfo_set_boundary.argtypes = [E, C.c_int, C.POINTER(abi.Boundary)]
         L.tfo_set_boundary_potential.argtypes = [E, C.c_int, C.c_int, abi.P_POT]
         L.tfo_set_species_flags.argtypes = [E, C.c_int, abi.U_P]
+        L.tfo_set_species_reset.argtypes = [E, C.c_int, abi.F_P]
         L.tfo_set_random_force.argtypes = [E, C.c_int, C.c_float, C.c_float, C.c_int]
         L.tfo_load_particles.argtypes = [E, C.c_int, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P,
                                          abi.U_P, abi.F_P, abi.F_P]
@@ -230,6 +231,10 @@ class OracleEngine:
 
     def set_random_force(self, t, mean, std, duration_steps):
         _chk(self.L.tfo_set_random_force(self.h, t, mean, std, duration_steps), "set_random_force")
+
+    def set_species_reset(self, values):
+        a = np.ascontiguousarray(values, np.float32)
+        _chk(self.L.tfo_set_species_reset(self.h, len(a), _fp(a)), "set_species_reset")
 
     def set_bonded_potential(self, slot, pot):
         _chk(self.L.tfo_set_bonded_potential(self.h, slot, pot), "set_bonded_potential")

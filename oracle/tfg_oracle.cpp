@@ -166,6 +166,7 @@ template <typename R> struct Engine {
     std::vector<float> rf_mean, rf_std;
     std::vector<int> rf_dur;
     std::vector<uint32_t> species_flags;
+    std::vector<float> species_reset;   // StateVector::reset values (state/tfStateVector.cpp:36-44)
     std::vector<float> svec;    // n * nspec (by id)
     std::vector<R> sq;          // n * nspec (by id)
     std::vector<Pot<R>> bpots;  // bonded slots
@@ -332,6 +333,7 @@ template <typename R> static int init_space(Engine<R> &e, const tfg_engine_desc 
     e.rf_std.assign(e.max_type, 0.f);
     e.rf_dur.assign(e.max_type, 1);
     e.species_flags.assign(std::max(1, e.nspec), 0u);
+    e.species_reset.assign(std::max(1, e.nspec), 0.f);
     e.wpots.assign(6 * e.max_type, Pot<R>());
     e.dt = d->dt;
     // dt_flux = dt / nr_fluxsteps (tfSimulator.cpp:653), an FP32 division
@@ -645,6 +647,27 @@ template <typename R> static bool on_wall(const Engine<R> &e, int w, const int *
     if (!(e.walls[w].kind & active)) return false;
     const int ax = w >> 1;
     return (w & 1) ? loc[ax] + 1 == e.cdim[ax] : loc[ax] == 0;
+}
+
+// Periodic wall flag of a cell along axis k (space_init, tfSpace.cpp:812-830): the low
+// wall's at index 0 when that wall is PERIODIC, else the high wall's at index cdim-1; -1 none.
+template <typename R> static int periodic_side(const Engine<R> &e, int k, int l) {
+    if (l == 0 && (e.walls[2 * k].kind & TFG_BOUNDARY_PERIODIC)) return 0;
+    if (l + 1 == e.cdim[k] && (e.walls[2 * k + 1].kind & TFG_BOUNDARY_PERIODIC)) return 1;
+    return -1;
+}
+
+// apply_boundary_particle_crossing (tfBoundaryConditions.cpp:676-735): for the axes whose
+// cell index changes, in order x, y, z, on a periodic axis, with both cells flagged periodic
+// on that axis, the destination's wall decides; the state vector is reset once.
+template <typename R> static bool crossing_resets(const Engine<R> &e, const int *src, const int *dst) {
+    for (int k = 0; k < 3; k++) {
+        if (src[k] == dst[k] || !((e.periodic >> k) & 1u)) continue;
+        const int ss = periodic_side(e, k, src[k]), ds = periodic_side(e, k, dst[k]);
+        if (ss < 0 || ds < 0) continue;
+        if (e.walls[2 * k + ds].kind & TFG_BOUNDARY_RESETTING) return true;
+    }
+    return false;
 }
 
 // boundary_eval (tf_boundary_eval.h:192-254) with boundary_potential_eval_ex (:146-188) and
@@ -1024,6 +1047,9 @@ template <typename R> static void advance_cell(Engine<R> &e, int cid, const floa
                               (c.loc[1] + delta[1] + e.cdim[1]) % e.cdim[1],
                               (c.loc[2] + delta[2] + e.cdim[2]) % e.cdim[2]);
             Cell<R> &cd = e.cells[dest];
+            // apply_boundary_particle_crossing (tfBoundaryConditions.cpp:676-735)
+            if (e.nspec > 0 && crossing_resets(e, c.loc, cd.loc))
+                for (int s = 0; s < e.nspec; s++) e.svec[(size_t)p.id * e.nspec + s] = e.species_reset[s];
             {
                 std::lock_guard<std::mutex> g(cd.mtx);
                 cd.incoming.push_back(p);
@@ -1372,10 +1398,11 @@ TFG_API int tfo_set_boundary(tfo_engine *eh, int wall, const tfg_boundary *bc) {
         for (int w = 0; w < 6; w++) e.walls[w] = e.walls_set[w];
         for (int ax = 0; ax < 3; ax++) {
             tfg_boundary &lo = e.walls[2 * ax], &hi = e.walls[2 * ax + 1];
-            if ((lo.kind & TFG_BOUNDARY_PERIODIC) || (hi.kind & TFG_BOUNDARY_PERIODIC)) {
-                lo.kind = hi.kind = TFG_BOUNDARY_PERIODIC;
-                e.periodic |= 1u << ax;
-            }
+            const bool pl = lo.kind & TFG_BOUNDARY_PERIODIC, ph = hi.kind & TFG_BOUNDARY_PERIODIC;
+            // only one of the two periodic: both become exactly PERIODIC; both periodic:
+            // their other bits (RESETTING) stay
+            if (pl != ph) lo.kind = hi.kind = TFG_BOUNDARY_PERIODIC;
+            if (pl || ph) e.periodic |= 1u << ax;
         }
         build_tasks(e);
         e.verlet_rebuild = true;
@@ -1405,6 +1432,15 @@ TFG_API int tfo_add_flux(tfo_engine *eh, int ti, int tj, const tfg_flux *f) {
         if ((int)L.size() >= TFG_MAX_FLUX_PER_PAIR - 1) return TFG_E_OVERFLOW;
         L.push_back(*f);
         if (ti != tj) e.fluxes[tj * e.max_type + ti] = L;
+        return TFG_OK;
+    };
+    return DISPATCH(h, go);
+}
+
+TFG_API int tfo_set_species_reset(tfo_engine *eh, int nr, const float *values) {
+    Handle *h = reinterpret_cast<Handle *>(eh);
+    auto go = [&](auto &e) {
+        for (int s = 0; s < nr && s < (int)e.species_reset.size(); s++) e.species_reset[s] = values[s];
         return TFG_OK;
     };
     return DISPATCH(h, go);

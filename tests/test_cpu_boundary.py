@@ -67,3 +67,56 @@ def test_wall_potential_force():
     # part.f -= f * dx with dx = +r for the low wall
     assert abs(f[0] - (-fr * r)) <= 1e-5 * max(1.0, abs(fr * r))
     assert f[1] == 0 and f[2] == 0
+
+
+def resetting_box():
+    """A periodic box whose x walls are PERIODIC | RESETTING: particles carry one species at
+    1.0 and drift at constant velocity; those crossing the x boundary take the reset value
+    0.25 (apply_boundary_particle_crossing, tfBoundaryConditions.cpp:676-735), those crossing
+    the plain periodic y boundary keep theirs."""
+    from tfg.configs import Workload
+    n = 40
+    rng = np.random.default_rng(3)
+    x = np.zeros((n, 3), np.float32)
+    v = np.zeros((n, 3), np.float32)
+    x[:20, 0] = rng.uniform(9.90, 9.98, 20)        # about to cross x = 10 in +x
+    x[:20, 1:] = rng.uniform(1.0, 9.0, (20, 2))
+    v[:20, 0] = 1.0
+    x[20:30, 0] = rng.uniform(0.02, 0.08, 10)      # about to cross x = 0 in -x
+    x[20:30, 1:] = rng.uniform(1.0, 9.0, (10, 2))
+    v[20:30, 0] = -1.0
+    x[30:, 1] = rng.uniform(9.90, 9.98, 10)        # about to cross y = 10 in +y (not resetting)
+    x[30:, [0, 2]] = rng.uniform(1.0, 9.0, (10, 2))
+    v[30:, 1] = 1.0
+    w = Workload(name="resetting_box", origin=(0.0, 0.0, 0.0), dim=(10.0,) * 3, cells=(3, 3, 3), cutoff=1.0,
+                 dt=0.01, steps=20, x=x, type=np.zeros(n, np.int32), v=v, radius=np.ones(n, np.float32),
+                 imass=np.ones(n, np.float32), species=np.ones((n, 1), np.float32), nr_species=1, max_type=1,
+                 dynamics=[abi.NEWTONIAN], mass=[1.0], flags=abi.ENGINE_NO_DENSITY)
+    kind = abi.BOUNDARY_PERIODIC | abi.BOUNDARY_RESETTING
+    w.boundaries = [(0, kind, (0, 0, 0), 1.0, 0.0), (1, kind, (0, 0, 0), 1.0, 0.0)]
+    w.species_reset = [0.25]
+    return w
+
+
+def test_resetting_boundary_resets_species_of_crossers_only():
+    from helpers import make_oracle
+    w = resetting_box()
+    e = make_oracle(w)
+    e.step(20)
+    d = e.download()
+    assert np.all(d["x"][:20, 0] < 1.0) and np.all(d["x"][20:30, 0] > 9.0)   # wrapped in x
+    assert np.all(d["species"][:30, 0] == np.float32(0.25))
+    assert np.all(d["x"][30:, 1] < 1.0)                                        # wrapped in y
+    assert np.all(d["species"][30:, 0] == 1.0)
+
+
+def test_resetting_needs_both_walls_periodic():
+    """A RESETTING wall facing a non-periodic one: check_periodicy makes both exactly
+    PERIODIC (tfBoundaryConditions.cpp:192-216), which drops RESETTING: nothing resets."""
+    from helpers import make_oracle
+    w = resetting_box()
+    w.boundaries = [(0, abi.BOUNDARY_PERIODIC | abi.BOUNDARY_RESETTING, (0, 0, 0), 1.0, 0.0),
+                    (1, abi.BOUNDARY_FREESLIP, (0, 0, 0), 1.0, 0.0)]
+    e = make_oracle(w)
+    e.step(20)
+    assert np.all(e.download()["species"][:, 0] == 1.0)

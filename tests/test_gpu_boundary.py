@@ -93,3 +93,19 @@ def test_boundaries_inside_a_batch():
         d = a["x"] - r["x"]
         d -= side * np.round(d / side)
         assert np.max(np.abs(d)) < 1e-3
+
+
+def test_resetting_boundary_matches_oracle():
+    """BOUNDARY_RESETTING on the GPU: with no pair forces the integrator is bit-exact, so
+    positions, cells and the species values (reset at the x crossings only) equal the
+    oracle's bit for bit."""
+    from test_cpu_boundary import resetting_box
+    w = resetting_box()
+    g, o = make_gpu(w), make_oracle(w)
+    g.step(20)
+    o.step(20)
+    a, b = g.download(), o.download()
+    assert np.array_equal(a["cell"], b["cell"])
+    assert np.array_equal(a["xrel"].view(np.uint32), b["xrel"].view(np.uint32))
+    assert np.array_equal(a["species"], b["species"])
+    assert np.all(a["species"][:30, 0] == np.float32(0.25)) and np.all(a["species"][30:, 0] == 1.0)

@@ -80,6 +80,32 @@ def test_every_work_split_matches(split):
     assert force_error(g.download()["f"], o.download()["f"], o.fmag()) < FORCE_RTOL
 
 
+@pytest.mark.parametrize("tuple_", [(1, 4, 1), (2, 8, 2), (7, 4, 4), (14, 8, 4), (1, 4, 8)])
+def test_every_tuning_tuple_matches(tuple_):
+    """Warps per CTA (8, or 4 for tabulated potentials) and work items per grab change only
+    the launch shape: the pair set stays bit-exact and the forces within tolerance."""
+    w = configs.cell_sorting()
+    g = make_gpu(w)
+    g.set_tuning(*tuple_)
+    assert g.tuning() == tuple_
+    o = make_oracle(w)
+    g.force_only()
+    o.force_only()
+    gc, gh = g.pair_signature()
+    oc, oh = o.signature()
+    assert np.array_equal(gc, oc) and np.array_equal(gh, oh)
+    assert force_error(g.download()["f"], o.download()["f"], o.fmag()) < FORCE_RTOL
+
+
+def test_autotune_picks_a_valid_tuple():
+    w = configs.cell_sorting()
+    g = make_gpu(w)
+    split = g.autotune()
+    t = g.tuning()
+    assert t[0] == split and split in (1, 2, 7, 14, abi.PAIR_HOME_OUTER)
+    assert t[1] in (4, 8) and t[2] in (1, 2, 4)
+
+
 def test_autotune_leaves_state_unchanged():
     w = small_dpd()
     g = make_gpu(w)

@@ -132,6 +132,15 @@ int set_species_flags(tfg_engine *eng, int sim, int nr, const uint32_t *flags) {
     return TFG_OK;
 }
 
+int set_species_reset(tfg_engine *eng, int sim, int nr, const float *values) {
+    int rc = sim_check(eng, sim);
+    if (rc) return rc;
+    if (nr < 0 || nr > kMaxSpecies || (nr && !values)) return TFG_E_INVAL;
+    for (int s = 0; s < nr; s++) eng->sims[sim].P.species_reset[s] = values[s];
+    eng->layout_dirty = true;   // parameters are uploaded with the layout
+    return TFG_OK;
+}
+
 int set_random_force(tfg_engine *eng, int sim, int type, float mean, float std_, int duration_steps) {
     int rc = sim_check(eng, sim);
     if (rc) return rc;
@@ -286,6 +295,12 @@ TFG_API int tfg_set_species_flags(tfg_engine *eng, int nr, const uint32_t *flags
 TFG_API int tfg_batch_set_species_flags(tfg_engine *eng, int sim, int nr, const uint32_t *flags) {
     return set_species_flags(eng, sim, nr, flags);
 }
+TFG_API int tfg_set_species_reset(tfg_engine *eng, int nr, const float *values) {
+    return set_species_reset(eng, 0, nr, values);
+}
+TFG_API int tfg_batch_set_species_reset(tfg_engine *eng, int sim, int nr, const float *values) {
+    return set_species_reset(eng, sim, nr, values);
+}
 TFG_API int tfg_set_random_force(tfg_engine *eng, int type, float mean, float std_, int duration_steps) {
     return set_random_force(eng, 0, type, mean, std_, duration_steps);
 }
@@ -407,31 +422,65 @@ TFG_API int tfg_force_only(tfg_engine *eng, int with_bonded) {
     return force_pass(eng, with_bonded != 0, false);
 }
 
-TFG_API int tfg_pair_signature(tfg_engine *eng, int32_t *count, uint32_t *hash) {
-    if (!eng || !count || !hash) return TFG_E_INVAL;
+// The pair pass's own walk and pair decision in signature mode (no forces): per-particle
+// partner count and id hash, and optionally the explicit pair list.
+static int signature_pass(tfg_engine *eng, int32_t *count, uint32_t *hash, int64_t cap, int32_t *pairs,
+                          int64_t *npairs) {
     int rc = commit(eng);
     if (rc) return rc;
     const int n = eng->n;
+    if (npairs) *npairs = 0;
     if (n == 0) return TFG_OK;
     if (eng->split == 0) eng->split = 1;
+    const int64_t pc = pairs ? std::max<int64_t>(cap, 0) : 0;
+    // signature words, then the pair counter (8-byte aligned), then the pair list
+    const size_t words = (size_t)2 * n + 2 + (size_t)2 * pc;
     int32_t *dbuf = nullptr;
-    rc = dalloc(eng, &dbuf, (size_t)2 * n);
+    rc = dalloc(eng, &dbuf, words + 1);
     if (rc) return rc;
+    int32_t *base = dbuf + (reinterpret_cast<uintptr_t>(dbuf) % 8 ? 1 : 0);
     PairKernelArgs a = pair_args(eng);
-    a.sig_count = dbuf;
-    a.sig_hash = reinterpret_cast<uint32_t *>(dbuf + n);
-    cudaMemsetAsync(dbuf, 0, sizeof(int32_t) * 2 * n, eng->stream);
+    a.sig_count = base;
+    a.sig_hash = reinterpret_cast<uint32_t *>(base + n);
+    unsigned long long *cnt_dev = reinterpret_cast<unsigned long long *>(base + 2 * (size_t)n + ((size_t)n % 2 ? 1 : 0));
+    if (pairs) {
+        a.pair_n = cnt_dev;
+        a.pair_out = reinterpret_cast<int32_t *>(cnt_dev + 1);
+        a.pair_cap = pc;
+    }
+    cudaMemsetAsync(dbuf, 0, sizeof(int32_t) * (words + 1), eng->stream);
     if (use_tile(eng))
         launch_pair_tile(a, tile_plan(eng, eng->split), eng->overflow_list, eng->overflow_count, eng->sms, true,
-                         eng->split, eng->stream);
+                         tune_of(eng), eng->stream);
     else
         launch_pair_signature(a, eng->stream);
-    cudaMemcpyAsync(count, a.sig_count, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, eng->stream);
-    cudaMemcpyAsync(hash, a.sig_hash, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, eng->stream);
+    if (count) cudaMemcpyAsync(count, a.sig_count, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, eng->stream);
+    if (hash) cudaMemcpyAsync(hash, a.sig_hash, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, eng->stream);
+    unsigned long long found = 0;
+    if (pairs) cudaMemcpyAsync(&found, cnt_dev, sizeof(found), cudaMemcpyDeviceToHost, eng->stream);
     cudaError_t e = cudaStreamSynchronize(eng->stream);
+    if (e == cudaSuccess && pairs && found) {
+        const size_t take = (size_t)std::min<int64_t>((int64_t)found, pc);
+        e = cudaMemcpy(pairs, a.pair_out, sizeof(int32_t) * 2 * take, cudaMemcpyDeviceToHost);
+    }
     cudaFree(dbuf);
     if (e != cudaSuccess) return fail(eng, TFG_E_CUDA, cudaGetErrorString(e));
+    if (npairs) *npairs = (int64_t)found;
     return check_launch(eng);
+}
+
+TFG_API int tfg_pair_signature(tfg_engine *eng, int32_t *count, uint32_t *hash) {
+    if (!eng || !count || !hash) return TFG_E_INVAL;
+    return signature_pass(eng, count, hash, 0, nullptr, nullptr);
+}
+
+TFG_API int tfg_pair_list(tfg_engine *eng, int64_t cap, int32_t *pairs, int64_t *count) {
+    if (!eng || !count || cap < 0 || (cap > 0 && !pairs)) return TFG_E_INVAL;
+    if (cap == 0) {   // count only: a one-pair buffer that is not copied out
+        int32_t dummy[2];
+        return signature_pass(eng, nullptr, nullptr, 1, dummy, count);
+    }
+    return signature_pass(eng, nullptr, nullptr, cap, pairs, count);
 }
 
 TFG_API int tfg_sync(tfg_engine *eng) {
@@ -487,6 +536,46 @@ TFG_API int tfg_get_verlet(tfg_engine *eng, int64_t *rebuilds, float *maxdx) {
     if (!eng) return TFG_E_INVAL;
     return verlet_sim(eng, 0, rebuilds, maxdx);
 }
+TFG_API int tfg_get_tuning(tfg_engine *eng, int *split, int *warps, int *grab) {
+    if (!eng) return TFG_E_INVAL;
+    if (split) *split = eng->split;
+    if (warps) *warps = eng->tune_warps;
+    if (grab) *grab = eng->tune_grab;
+    return TFG_OK;
+}
+
+TFG_API int tfg_set_tuning(tfg_engine *eng, int split, int warps, int grab) {
+    if (!eng || !(split == 1 || split == 2 || split == 7 || split == 14 || split == TFG_PAIR_HOME_OUTER) ||
+        !(warps == 4 || warps == 8) || grab < 1 || grab > 8)
+        return TFG_E_INVAL;
+    eng->split = split;
+    eng->tune_warps = warps;
+    eng->tune_grab = grab;
+    eng->gen++;
+    return TFG_OK;
+}
+
+TFG_API int tfg_set_deterministic(tfg_engine *eng, int enable) {
+    if (!eng) return TFG_E_INVAL;
+    if (eng->deterministic != (enable != 0)) {
+        eng->deterministic = enable != 0;
+        eng->gen++;
+    }
+    return TFG_OK;
+}
+
+TFG_API int tfg_batch_resume(tfg_engine *eng, int sim, int64_t steps, const float *q) {
+    int rc = sim_check(eng, sim);
+    if (rc) return rc;
+    SimHost &S = eng->sims[sim];
+    if (steps < 0) return fail(eng, TFG_E_INVAL, "negative step count");
+    if (!S.pending) return fail(eng, TFG_E_STATE, "resume applies to particles loaded since the last step");
+    S.time = steps;
+    if (q) S.q_pending.assign(q, q + (size_t)S.n * eng->nspec);
+    else S.q_pending.clear();
+    return TFG_OK;
+}
+
 TFG_API int tfg_batch_sim_status(tfg_engine *eng, int sim, int *status) {
     if (!eng) return TFG_E_INVAL;
     return sim_status(eng, sim, status);

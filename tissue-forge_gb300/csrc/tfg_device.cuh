@@ -89,6 +89,7 @@ struct SimParams {
     float4 wall_vel[6];      // wall velocity; w = restore
     float wall_radius[6];
     int32_t wpot_base;       // (wall 0, type 0) in the wall-potential array; walls x types
+    float species_reset[kMaxSpecies];  // species values after crossing a RESETTING wall
     // Verlet mode (TFG_ENGINE_VERLET; engine_verlet_update, tfEngine.cpp:214-354).  The
     // device fields are written by k_tick and k_advance; the host writes 2 to
     // verlet_rebuild to force a rebuild at the next step.
@@ -99,6 +100,29 @@ struct SimParams {
     float verlet_maxdx;      // device: largest displacement at the last check (0 on a rebuild)
     int64_t verlet_rebuilds; // device: rebuilds so far
 };
+
+// Does a particle that moves by delta[] from the cell at loc[] cross a RESETTING wall?
+// apply_boundary_particle_crossing (tfBoundaryConditions.cpp:676-735): along each axis in
+// order x, y, z whose cell index changes, on a periodic axis, both cells must carry the
+// periodic wall flag of their side (space_init: a cell at index 0 takes the low wall's flag
+// when that wall is PERIODIC, else a cell at index cdim-1 the high wall's), and the
+// destination's wall must be RESETTING.
+__host__ __device__ inline bool crosses_resetting_wall(const SimParams &P, const int loc[3], const int delta[3]) {
+    for (int k = 0; k < 3; k++) {
+        if (delta[k] == 0 || !((P.periodic >> k) & 1u)) continue;
+        const int n = P.cdim[k];
+        const int src = loc[k], dst = (loc[k] + delta[k] + n) % n;
+        auto side = [&](int l) {   // 0 low wall flag, 1 high wall flag, -1 none
+            if (l == 0 && (P.wall_kind[2 * k] & TFG_BOUNDARY_PERIODIC)) return 0;
+            if (l + 1 == n && (P.wall_kind[2 * k + 1] & TFG_BOUNDARY_PERIODIC)) return 1;
+            return -1;
+        };
+        const int ss = side(src), ds = side(dst);
+        if (ss < 0 || ds < 0) continue;
+        if (P.wall_kind[2 * k + ds] & TFG_BOUNDARY_RESETTING) return true;
+    }
+    return false;
+}
 
 // Is wall w of this simulation active and is cell location (a, b, c) on it?
 __host__ __device__ inline bool on_wall(const SimParams &P, int w, int a, int b, int c) {

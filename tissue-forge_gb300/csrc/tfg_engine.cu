@@ -74,8 +74,18 @@ int upload_pending(tfg_engine *eng, SimHost &S, ParticleArrays &D, int cap) {
         if (!S.species.empty())
             for (int i = 0; i < n; i++) col[i] = S.species[(size_t)i * eng->nspec + k];
         CK(cudaMemcpyAsync(D.sval + (size_t)k * cap + slot0, col.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s));
-        CK(cudaMemsetAsync(D.sq + (size_t)k * cap + slot0, 0, sizeof(float) * n, s));
+        if (S.q_pending.size() == (size_t)n * eng->nspec) {
+            // a resumed simulation keeps the increments its migrants carry to the next step
+            std::vector<float> qc(n);
+            for (int i = 0; i < n; i++) qc[i] = S.q_pending[(size_t)i * eng->nspec + k];
+            CK(cudaMemcpyAsync(D.sq + (size_t)k * cap + slot0, qc.data(), sizeof(float) * n, cudaMemcpyHostToDevice,
+                               s));
+        } else {
+            CK(cudaMemsetAsync(D.sq + (size_t)k * cap + slot0, 0, sizeof(float) * n, s));
+        }
     }
+    CK(cudaStreamSynchronize(s));
+    S.q_pending.clear();
     if (!S.pending_binned) {
         float *dx = nullptr;
         int32_t *dtype = nullptr;
@@ -520,10 +530,9 @@ void resolve_boundaries(SimHost &S) {
     uint32_t kind[6];
     for (int w = 0; w < 6; w++) kind[w] = S.walls[w].kind;
     for (int ax = 0; ax < 3; ax++) {
-        if ((kind[2 * ax] | kind[2 * ax + 1]) & TFG_BOUNDARY_PERIODIC) {
-            kind[2 * ax] = kind[2 * ax + 1] = TFG_BOUNDARY_PERIODIC;
-            P.periodic |= 1u << ax;
-        }
+        const bool lo = kind[2 * ax] & TFG_BOUNDARY_PERIODIC, hi = kind[2 * ax + 1] & TFG_BOUNDARY_PERIODIC;
+        if (lo != hi) kind[2 * ax] = kind[2 * ax + 1] = TFG_BOUNDARY_PERIODIC;
+        if (lo || hi) P.periodic |= 1u << ax;
     }
     const uint32_t active = TFG_BOUNDARY_FREESLIP | TFG_BOUNDARY_VELOCITY | TFG_BOUNDARY_POTENTIAL;
     for (int w = 0; w < 6; w++) {
@@ -692,6 +701,7 @@ int load_sim(tfg_engine *eng, int sim, int n, const float *xg, const int32_t *ce
     S.loaded = true;
     S.pending = true;
     S.time = 0;
+    S.q_pending.clear();
     S.P.verlet_rebuilds = 0;
     S.P.verlet_maxdx = 0.f;
     eng->layout_dirty = true;
@@ -886,7 +896,7 @@ const TilePlan &tile_plan(tfg_engine *eng, int split) {
 }
 
 // The tiled half-shell kernel handles at most one species; more go to the stencil kernel.
-bool use_tile(const tfg_engine *eng) { return !(eng->has_flux && eng->nspec > 1); }
+bool use_tile(const tfg_engine *eng) { return !eng->deterministic && !(eng->has_flux && eng->nspec > 1); }
 
 int force_pass(tfg_engine *eng, bool bonded, bool timed) {
     cudaStream_t s = eng->stream;
@@ -895,7 +905,7 @@ int force_pass(tfg_engine *eng, bool bonded, bool timed) {
     if (eng->n > 0) {
         if (use_tile(eng))
             launch_pair_tile(a, tile_plan(eng, eng->split), eng->overflow_list, eng->overflow_count, eng->sms, false,
-                             eng->split, s);
+                             tune_of(eng), s);
         else launch_pair(a, s);
     }
     if (timed) launch_stamp(eng->stamps, 2, s);
@@ -1027,26 +1037,44 @@ int autotune(tfg_engine *eng) {
     int rc = dalloc(eng, &save, nq);
     if (rc) return rc;
     CK(cudaMemcpyAsync(save, eng->A[eng->cur].sq, sizeof(float) * nq, cudaMemcpyDeviceToDevice, s));
-    const int cand[5] = {1, 2, 7, 14, TFG_PAIR_HOME_OUTER};
-    const int ncand = pair_home_eligible(pair_args(eng)) ? 5 : 4;
+    // candidates: every work split of the tiled kernel with 1, 2 or 4 items per grab, in CTAs
+    // of 8 warps and, for the table variants, of 4; and the home-outer kernel
+    const PairKernelArgs a0 = pair_args(eng);
+    const bool table_only = !a0.has_dpd && !(a0.nspec > 0 && a0.has_flux);
+    std::vector<TileTune> cand;
+    for (int split : {1, 2, 7, 14})
+        for (int warps : {8, 4})
+            for (int grab : {1, 2, 4}) {
+                if (warps == 4 && !table_only) continue;
+                TileTune t;
+                t.split = split;
+                t.warps = warps;
+                t.grab = grab;
+                cand.push_back(t);
+            }
+    if (pair_home_eligible(a0)) {
+        TileTune t;
+        t.split = TFG_PAIR_HOME_OUTER;
+        cand.push_back(t);
+    }
     float best = 1e30f;
-    int best_split = 1;
-    for (int c = 0; c < ncand; c++) {
+    TileTune best_t;
+    for (const TileTune &tc : cand) {
         float tmin = 1e30f;
         for (int rep = 0; rep < 3; rep++) {
             rc = bin(eng, 0);
             if (rc) { cudaFree(save); return rc; }
             PairKernelArgs a = pair_args(eng);
             cudaEventRecord(eng->ev[0], s);
-            launch_pair_tile(a, tile_plan(eng, cand[c]), eng->overflow_list, eng->overflow_count, eng->sms, false,
-                             cand[c], s);
+            launch_pair_tile(a, tile_plan(eng, tc.split), eng->overflow_list, eng->overflow_count, eng->sms, false,
+                             tc, s);
             cudaEventRecord(eng->ev[1], s);
             CK(cudaEventSynchronize(eng->ev[1]));
             float ms = 0.f;
             cudaEventElapsedTime(&ms, eng->ev[0], eng->ev[1]);
             tmin = std::min(tmin, ms);
         }
-        if (tmin < best) { best = tmin; best_split = cand[c]; }
+        if (tmin < best) { best = tmin; best_t = tc; }
     }
     CK(cudaMemcpyAsync(eng->A[eng->cur].sq, save, sizeof(float) * nq, cudaMemcpyDeviceToDevice, s));
     CK(cudaStreamSynchronize(s));
@@ -1054,7 +1082,9 @@ int autotune(tfg_engine *eng) {
     rc = bin(eng, 0);
     if (rc) return rc;
     CK(cudaStreamSynchronize(s));
-    eng->split = best_split;
+    eng->split = best_t.split;
+    eng->tune_warps = best_t.warps;
+    eng->tune_grab = best_t.grab;
     eng->gen++;
     return check_launch(eng);
 }

@@ -46,6 +46,7 @@ struct SimHost {
     std::vector<tfg::PotDev> wpots;  // 6 x max_type wall potentials
     std::vector<std::vector<float>> wtables;
     int status = 0;                  // first error of this simulation (TFG_E_*), sticky
+    std::vector<float> q_pending;    // flux increments to restore at the next layout (id order)
 };
 
 struct tfg_engine {
@@ -118,6 +119,9 @@ struct tfg_engine {
     int max_fluxsteps = 1;           // largest nr_fluxsteps of a simulation with fluxes
     uint32_t flags_all = 0;          // TFG_ENGINE_NO_DENSITY only when every simulation sets it
     int split = 0;                   // tiled pair pass: warps per home cell (0 = not tuned)
+    int tune_warps = 8;              // tiled pair pass: warps per CTA (table variants: 8 or 4)
+    int tune_grab = 1;               // tiled pair pass: work items per grab
+    bool deterministic = false;      // pair pass without atomics (stencil kernel): reproducible bits
     int capacity_hint = 0;
     // tiled-pass staging plan, cached for (generation, split)
     tfg::TilePlan plan;
@@ -165,6 +169,13 @@ int flux_substeps(tfg_engine *eng);  // one_step without the host clock
 int graph_step(tfg_engine *eng);                // one step replayed from a captured graph
 int run_steps(tfg_engine *eng, int nsteps);     // nsteps steps, graphs where they apply
 int autotune(tfg_engine *eng);
+inline TileTune tune_of(const tfg_engine *eng) {
+    TileTune t;
+    t.split = eng->split;
+    t.warps = eng->tune_warps;
+    t.grab = eng->tune_grab;
+    return t;
+}
 int prepare_lists(tfg_engine *eng, bool relaid);  // allocate / invalidate the Verlet pair lists
 int check_lists(tfg_engine *eng);                 // grow them when a build asked for more
 PairKernelArgs pair_args(tfg_engine *eng);

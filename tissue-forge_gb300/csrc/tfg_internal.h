@@ -69,6 +69,9 @@ struct PairKernelArgs {
     uint32_t *err;
     int32_t *sig_count;         // signature mode: interacting neighbours per particle
     uint32_t *sig_hash;         // signature mode: order-independent hash of neighbour ids
+    int32_t *pair_out;          // signature mode, optional: (lower id, higher id) of each pair found
+    unsigned long long *pair_n; // pairs found (the first pair_cap are written)
+    long long pair_cap;
     int flux_sub;               // >= 0: flux-only substep pass number (simulations with
                                 // nr_fluxsteps - 1 > flux_sub take part); -1: the full pass
     bool has_dpd;               // any type pair uses a DPD potential
@@ -99,8 +102,17 @@ struct TilePlan {
     int stage_pots = 0;
 };
 TilePlan plan_pair_tile(int nsims, int max_type, int blob_floats);
+// Launch configuration of the nonbonded pass, picked by the autotuner: the work split (warps
+// per home cell: 1, 2, 7 or 14, or TFG_PAIR_HOME_OUTER for the home-outer kernel), the
+// warps per CTA of the tiled kernel's table variants (8, or 4 with twice the CTAs per SM),
+// and the work items a warp takes from the shared counter at a time.
+struct TileTune {
+    int split = 1;
+    int warps = 8;
+    int grab = 1;
+};
 void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overflow_list, int *overflow_count, int sms,
-                      bool signature, int split, cudaStream_t s);
+                      bool signature, const TileTune &tune, cudaStream_t s);
 // Overflow pass of the tiled kernels' table variant: the home cells listed in
 // overflow_list[0 .. overflow_count[0]), one warp each, global-memory candidates and atomics.
 void launch_pair_overflow(const PairKernelArgs &a, int *overflow_list, int *overflow_count, bool signature, int sms,
@@ -121,6 +133,16 @@ void launch_pair_fluxonly(const PairKernelArgs &a, const TilePlan &plan, int *ov
 // Same stencil walk and pair decision as launch_pair, writing only the per-particle
 // pair signature (used to prove the pair set bit-exact against the oracle).
 void launch_pair_signature(const PairKernelArgs &a, cudaStream_t s);
+
+// Signature mode with an explicit list: append the pair (ida, idb) once.
+__device__ __forceinline__ void record_pair(const PairKernelArgs &a, int ida, int idb) {
+    if (!a.pair_out) return;
+    const unsigned long long p = atomicAdd(a.pair_n, 1ull);
+    if ((long long)p < a.pair_cap) {
+        a.pair_out[2 * p] = ida < idb ? ida : idb;
+        a.pair_out[2 * p + 1] = ida < idb ? idb : ida;
+    }
+}
 
 // Hash of one neighbour id for the pair signature.
 __host__ __device__ inline uint32_t sig_mix(uint32_t id) {

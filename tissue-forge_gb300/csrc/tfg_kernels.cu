@@ -600,6 +600,11 @@ __global__ void k_advance(int n, int cap, int nspec, SimParams *sims, const int3
                                      (c + delta[2] + P.cdim[2]) % P.cdim[2]);
                 migrated = true;
                 mig = 1.f;
+                if (nspec > 0) {
+                    const int loc[3] = {a, b, c};
+                    if (crosses_resetting_wall(P, loc, delta))
+                        for (int s = 0; s < nspec; s++) sval[s * cap + i] = P.species_reset[s];
+                }
             }
             if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]))) {
                 atomicOr(err, ERR_NAN);

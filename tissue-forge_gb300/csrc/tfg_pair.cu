@@ -160,7 +160,9 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
             if (r2 > P.cutoff2) continue;
             if (kSig) {
                 sig_n++;
-                sig_h += sig_mix((uint32_t)__float_as_int(a.aux[j].w));
+                const int idj = __float_as_int(a.aux[j].w);
+                sig_h += sig_mix((uint32_t)idj);
+                if (idi < idj) record_pair(a, idi, idj);
                 continue;
             }
             const float r = __fsqrt_rn(r2);

@@ -265,6 +265,7 @@ __global__ void __launch_bounds__(kHW * 32, 2) k_pair_home(HomeArgs T) {
                                 uint32_t *hk2 = reinterpret_cast<uint32_t *>(&S.acc[k].y);
                                 *ck += 1;
                                 *hk2 += sig_mix(idi);
+                                record_pair(a, (int)idi, (int)idk);
                             } else {
                                 float4 fK = make_float4(0.f, 0.f, 0.f, 0.f);
                                 if (kDensity) {

@@ -29,7 +29,6 @@ constexpr int kCapT = 156;          // staged particles per warp (table variants
 constexpr int kCapX = 88;           // staged particles per warp (DPD and flux variants)
 constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
 constexpr int kQ = 64;              // candidate ring queue entries per warp (power of two)
-constexpr int kGrab = 1;            // work items a warp takes from the shared counter at a time
 constexpr int kMaxSmemTable = 4096; // floats of potential table staged per CTA
 constexpr int kMaxSmemPots = 64;    // potential descriptors staged per CTA (all simulations)
 constexpr size_t kFourCtaBytes = 228 * 1024 / 4 - 1024;   // dynamic shared memory of a CTA, four per SM
@@ -78,6 +77,7 @@ struct TileArgs {
     int *overflow_list;    // home cells handed to the overflow kernel
     int *overflow_count;   // [0] overflow cells, [1] work counter of the tiled pass
     int split;             // warps per home cell: the 14 tasks are divided into `split` groups
+    int grab;              // work items a warp takes from the shared counter at a time
     int stage_floats;      // table floats and descriptors staged per CTA (TilePlan)
     int stage_pots;
 };
@@ -190,6 +190,7 @@ __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P
             const uint32_t idk = (uint32_t)__float_as_int(T.a.aux[S.gslot[K]].w);
             atomicAdd(reinterpret_cast<unsigned *>(&S.acc[I].y), sig_mix(idk));
             atomicAdd(reinterpret_cast<unsigned *>(&S.acc[K].y), sig_mix(idi));
+            record_pair(T.a, (int)idi, (int)idk);
         }
         return;
     }
@@ -359,13 +360,13 @@ __device__ __forceinline__ void flush(const PairKernelArgs &a, ST &S, int b0, in
 // pairs within the list radius of every staged chunk, and on the other steps evaluate
 // those lists instead of testing every candidate pair (engine_flag_verlet; the reference
 // keeps its sorted windows between rebuilds instead, tf_runner_dopair.cpp:115-117).
-template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false>
-__global__ void __launch_bounds__(kWarps * 32, 4) k_pair_tile(TileArgs T) {
+template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false, int kW = kWarps>
+__global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
     using Staged = typename TileOf<kDPD, kFlux>::S;
     constexpr int kCap = Staged::cap;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Staged *L = reinterpret_cast<Staged *>(smem_raw);
-    PotDev *spot_smem = reinterpret_cast<PotDev *>(smem_raw + sizeof(Staged) * kWarps);
+    PotDev *spot_smem = reinterpret_cast<PotDev *>(smem_raw + sizeof(Staged) * kW);
     float *sblob = reinterpret_cast<float *>(spot_smem + T.stage_pots);
     const PairKernelArgs &a = T.a;
 
@@ -388,13 +389,15 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_pair_tile(TileArgs T) {
     const int per = 14 / T.split;
     const int nitems = a.ncells * T.split;
 
-    // warps take items (home cell x task group) from a shared counter, kGrab at a time, so
+    // warps take items (home cell x task group) from a shared counter, T.grab at a time, so
     // that uneven cells (empty ones, droplet interiors) balance dynamically
+    const int grab = T.grab;
     int base = 0;
-    if (lane == 0) base = atomicAdd(T.overflow_count + 1, kGrab);
+    if (lane == 0) base = atomicAdd(T.overflow_count + 1, grab);
     base = __shfl_sync(0xffffffffu, base, 0);
     for (; base < nitems;) {
-    for (int item = base; item < base + kGrab && item < nitems; item++) {
+#pragma unroll 1
+    for (int item = base; item < base + grab && item < nitems; item++) {
         const int home = item / T.split, grp = item - home * T.split;
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         if (nh == 0) continue;
@@ -654,7 +657,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4) k_pair_tile(TileArgs T) {
         }
         __syncwarp();
     }
-    if (lane == 0) base = atomicAdd(T.overflow_count + 1, kGrab);
+    if (lane == 0) base = atomicAdd(T.overflow_count + 1, grab);
     base = __shfl_sync(0xffffffffu, base, 0);
     }
     if (kSig) return;
@@ -720,6 +723,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                     atomicAdd(&a.sig_count[__float_as_int(axj.w)], 1);
                     atomicAdd(&a.sig_hash[__float_as_int(axi.w)], sig_mix((uint32_t)__float_as_int(axj.w)));
                     atomicAdd(&a.sig_hash[__float_as_int(axj.w)], sig_mix((uint32_t)__float_as_int(axi.w)));
+                    record_pair(a, __float_as_int(axi.w), __float_as_int(axj.w));
                     continue;
                 }
                 const float r = __fsqrt_rn(r2);
@@ -794,15 +798,16 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
     }
 }
 
-template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false>
+template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false, int kW = kWarps>
 void launch_variant(const TileArgs &T0, cudaStream_t s, int sms) {
-    const size_t base = sizeof(typename TileOf<kDPD, kFlux>::S) * kWarps;
+    const size_t base = sizeof(typename TileOf<kDPD, kFlux>::S) * kW;
     const size_t smem_max = base + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxSmemPots;
-    // Tables and descriptors are staged only while a CTA still fits four per SM: the fourth
-    // CTA is worth more than shared-memory tables (the table variants' staging alone takes
-    // 56 KB, so their tables are always read through L1)
+    // Tables and descriptors are staged only while a CTA still fits 32 / kW per SM (four of 8
+    // warps): those CTAs are worth more than shared-memory tables (the table variants' staging
+    // alone takes 56 KB per 8 warps, so their tables are always read through L1)
+    const size_t cta_budget = kFourCtaBytes * kW / kWarps;
     TileArgs T = T0;
-    if (base + sizeof(PotDev) * T.stage_pots + sizeof(float) * ((T.stage_floats + 3) & ~3) > kFourCtaBytes) {
+    if (base + sizeof(PotDev) * T.stage_pots + sizeof(float) * ((T.stage_floats + 3) & ~3) > cta_budget) {
         T.stage_floats = 0;
         T.stage_pots = 0;
     }
@@ -811,19 +816,19 @@ void launch_variant(const TileArgs &T0, cudaStream_t s, int sms) {
     static size_t occ_smem = 0;
     static int per_sm = 1;
     if (!configured) {
-        cudaFuncSetAttribute(k_pair_tile<kDPD, kFlux, kDensity, kSig, kVerlet>,
+        cudaFuncSetAttribute(k_pair_tile<kDPD, kFlux, kDensity, kSig, kVerlet, kW>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
         configured = true;
     }
     if (occ_smem != smem) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_tile<kDPD, kFlux, kDensity, kSig, kVerlet>,
-                                                      kWarps * 32, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pair_tile<kDPD, kFlux, kDensity, kSig, kVerlet, kW>,
+                                                      kW * 32, smem);
         if (per_sm < 1) per_sm = 1;
         occ_smem = smem;
     }
-    const int want = (T.a.ncells * T.split + kWarps - 1) / kWarps;
+    const int want = (T.a.ncells * T.split + kW - 1) / kW;
     const int grid = std::max(1, std::min(want, sms * per_sm));
-    k_pair_tile<kDPD, kFlux, kDensity, kSig, kVerlet><<<grid, kWarps * 32, smem, s>>>(T);
+    k_pair_tile<kDPD, kFlux, kDensity, kSig, kVerlet, kW><<<grid, kW * 32, smem, s>>>(T);
     k_pair_overflow<kDPD, kFlux, kDensity, kSig><<<sms, 256, 0, s>>>(T);
 }
 
@@ -838,6 +843,7 @@ void launch_pair_overflow(const PairKernelArgs &a, int *overflow_list, int *over
     T.overflow_list = overflow_list;
     T.overflow_count = overflow_count;
     T.split = 1;
+    T.grab = 1;
     T.stage_floats = 0;
     T.stage_pots = 0;
     if (signature) k_pair_overflow<false, false, false, true><<<sms, 256, 0, s>>>(T);
@@ -856,6 +862,7 @@ void launch_pair_fluxonly(const PairKernelArgs &a, const TilePlan &plan, int *ov
     T.overflow_list = overflow_list;
     T.overflow_count = overflow_count;
     T.split = 1;
+    T.grab = 1;
     T.stage_floats = plan.stage_floats;
     T.stage_pots = plan.stage_pots;
     cudaMemsetAsync(overflow_count, 0, 2 * sizeof(int), s);
@@ -873,12 +880,14 @@ TilePlan plan_pair_tile(int nsims, int max_type, int blob_floats) {
 }
 
 void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overflow_list, int *overflow_count, int sms,
-                      bool signature, int split, cudaStream_t s) {
+                      bool signature, const TileTune &tune, cudaStream_t s) {
+    const int split = tune.split;
     TileArgs T;
     T.a = a;
     T.overflow_list = overflow_list;
     T.overflow_count = overflow_count;
     T.split = (split == 1 || split == 2 || split == 7 || split == 14) ? split : 1;
+    T.grab = tune.grab >= 1 && tune.grab <= 8 ? tune.grab : 1;
     T.stage_floats = plan.stage_floats;
     T.stage_pots = plan.stage_pots;
     cudaMemsetAsync(overflow_count, 0, 2 * sizeof(int), s);
@@ -897,6 +906,11 @@ void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overfl
     if (a.vlist && !dpd && !flux) {   // Verlet pair lists (some simulation in Verlet mode)
         if (dens) launch_variant<false, false, true, false, true>(T, s, sms);
         else launch_variant<false, false, false, false, true>(T, s, sms);
+        return;
+    }
+    if (!dpd && !flux && tune.warps == 4) {   // the table variants also come in CTAs of 4 warps
+        if (dens) launch_variant<false, false, true, false, false, 4>(T, s, sms);
+        else launch_variant<false, false, false, false, false, 4>(T, s, sms);
         return;
     }
 #define TFG_PAIR_DISPATCH(D, F)                                          \

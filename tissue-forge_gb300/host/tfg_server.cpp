@@ -66,6 +66,7 @@ struct tfg_request {
     std::vector<std::unique_ptr<Pair>> pots;
     std::vector<FluxAdd> fluxes;
     std::vector<uint32_t> species_flags;
+    std::vector<float> species_reset;
     std::vector<RForce> rforces;
     std::vector<Wall> walls;
     std::vector<std::unique_ptr<WallPot>> wall_pots;
@@ -177,6 +178,9 @@ int replay(tfg_engine *b, tfg_request &q, int *sim_out) {
         if ((rc = tfg_batch_add_flux(b, sim, f.ti, f.tj, &f.f))) return rc;
     if (!q.species_flags.empty() &&
         (rc = tfg_batch_set_species_flags(b, sim, (int)q.species_flags.size(), q.species_flags.data())))
+        return rc;
+    if (!q.species_reset.empty() &&
+        (rc = tfg_batch_set_species_reset(b, sim, (int)q.species_reset.size(), q.species_reset.data())))
         return rc;
     for (const auto &r : q.rforces)
         if ((rc = tfg_batch_set_random_force(b, sim, r.type, r.mean, r.std, r.dur))) return rc;
@@ -320,6 +324,37 @@ int complete_chunk(tfg_server *S, Lane &L) {
     return done + (int)fin.size();
 }
 
+// Start the next chunk on every idle batch with simulations: the quantum, cut at the
+// nearest finishing simulation.  Returns the requests retired on the way (zero-step
+// requests, or a chunk that failed to start).
+int launch_idle(tfg_server *S) {
+    int done = 0;
+    for (auto &kv : S->lanes) {
+        Lane &L = kv.second;
+        if (L.running || L.active.empty()) continue;
+        int chunk = S->desc.quantum;
+        for (auto &a : L.active) chunk = std::min(chunk, a.second.remaining);
+        if (chunk <= 0) {   // zero-step requests finish at once
+            L.running = 0;
+            L.in_chunk.clear();
+            done += complete_chunk(S, L);
+            continue;
+        }
+        L.in_chunk.clear();
+        for (auto &a : L.active) L.in_chunk.insert(a.first);
+        L.running = chunk;
+        const int rs = tfg_batch_step(L.batch, chunk);
+        S->st.chunks++;
+        if (rs != TFG_OK) {
+            // the chunk did not run as a whole: no steps are accounted, the failed leave
+            L.running = 0;
+            L.in_chunk.clear();
+            done += handle_error(S, L, rs);
+        }
+    }
+    return done;
+}
+
 }  // namespace
 
 extern "C" {
@@ -389,6 +424,12 @@ TFG_API int tfg_request_add_flux(tfg_request *q, int ti, int tj, const tfg_flux 
 TFG_API int tfg_request_set_species_flags(tfg_request *q, int nr, const uint32_t *flags) {
     if (!q || nr < 0 || (nr > 0 && !flags)) return TFG_E_INVAL;
     q->species_flags.assign(flags, flags + nr);
+    return TFG_OK;
+}
+
+TFG_API int tfg_request_set_species_reset(tfg_request *q, int nr, const float *values) {
+    if (!q || nr < 0 || (nr > 0 && !values)) return TFG_E_INVAL;
+    q->species_reset.assign(values, values + nr);
     return TFG_OK;
 }
 
@@ -481,40 +522,26 @@ TFG_API int tfg_server_poll(tfg_server *S, int wait_us, int *completed) {
     if (!S) return TFG_E_INVAL;
     int done = 0;
     int rc = admit(S);
-    for (auto &kv : S->lanes) {
-        Lane &L = kv.second;
-        if (L.running || L.active.empty()) continue;
-        int chunk = S->desc.quantum;
-        for (auto &a : L.active) chunk = std::min(chunk, a.second.remaining);
-        if (chunk <= 0) {   // zero-step requests finish at once
-            L.running = 0;
-            L.in_chunk.clear();
-            done += complete_chunk(S, L);
-            continue;
-        }
-        L.in_chunk.clear();
-        for (auto &a : L.active) L.in_chunk.insert(a.first);
-        L.running = chunk;
-        const int rs = tfg_batch_step(L.batch, chunk);
-        S->st.chunks++;
-        if (rs != TFG_OK) {
-            // the chunk did not run as a whole: no steps are accounted, the failed leave
-            L.running = 0;
-            L.in_chunk.clear();
-            done += handle_error(S, L, rs);
-        }
-    }
+    if (rc == TFG_OK) done += launch_idle(S);
     const auto deadline = Clock::now() + std::chrono::microseconds(std::max(0, wait_us));
     for (;;) {
         bool any_running = false;
+        int now_done = 0;
         for (auto &kv : S->lanes) {
             Lane &L = kv.second;
             if (!L.running) continue;
             int idle = 0;
-            if (tfg_query(L.batch, &idle) != TFG_OK || idle) done += complete_chunk(S, L);
+            if (tfg_query(L.batch, &idle) != TFG_OK || idle) now_done += complete_chunk(S, L);
             else any_running = true;
         }
-        if (done > 0 || !any_running || Clock::now() >= deadline) break;
+        if (now_done > 0) {
+            // slots and memory freed: admit the waiting requests and start the next chunks
+            done += now_done;
+            if (rc == TFG_OK) rc = admit(S);
+            if (rc == TFG_OK) done += launch_idle(S);
+            break;
+        }
+        if (!any_running || Clock::now() >= deadline) break;
         std::this_thread::sleep_for(std::chrono::microseconds(100));
     }
     S->st.queued = (int64_t)S->arrived.size();

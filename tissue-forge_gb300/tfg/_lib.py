@@ -37,6 +37,8 @@ def lib():
     L.tfg_set_potential.argtypes = [E, C.c_int, C.c_int, abi.P_POT]
     L.tfg_add_flux.argtypes = [E, C.c_int, C.c_int, C.POINTER(abi.Flux)]
     L.tfg_set_species_flags.argtypes = [E, C.c_int, abi.U_P]
+    L.tfg_set_species_reset.argtypes = [E, C.c_int, abi.F_P]
+    L.tfg_batch_set_species_reset.argtypes = [E, C.c_int, C.c_int, abi.F_P]
     L.tfg_set_random_force.argtypes = [E, C.c_int, C.c_float, C.c_float, C.c_int]
     L.tfg_load_particles.argtypes = [E, C.c_int, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P, abi.U_P, abi.F_P,
                                      abi.F_P]
@@ -51,8 +53,11 @@ def lib():
     L.tfg_query.argtypes = [E, C.POINTER(C.c_int)]
     L.tfg_set_graphs.argtypes = [E, C.c_int]
     L.tfg_pair_signature.argtypes = [E, abi.I_P, abi.U_P]
+    L.tfg_pair_list.argtypes = [E, C.c_int64, abi.I_P, C.POINTER(C.c_int64)]
     L.tfg_autotune.argtypes = [E, C.POINTER(C.c_int)]
     L.tfg_set_split.argtypes = [E, C.c_int]
+    L.tfg_get_tuning.argtypes = [E, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.tfg_set_tuning.argtypes = [E, C.c_int, C.c_int, C.c_int]
     L.tfg_get_count.argtypes = [E, C.POINTER(C.c_int)]
     L.tfg_download.argtypes = [E, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P, abi.F_P]
     L.tfg_get_reductions.argtypes = [E, C.POINTER(abi.Reductions)]
@@ -88,5 +93,9 @@ def lib():
                                      abi.F_P]
     L.tfg_batch_get_reductions.argtypes = [E, C.c_int, C.POINTER(abi.Reductions)]
     L.tfg_batch_get_verlet.argtypes = [E, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_float)]
+    L.tfg_batch_sim_status.argtypes = [E, C.c_int, C.POINTER(C.c_int)]
+    L.tfg_batch_resume.argtypes = [E, C.c_int, C.c_int64, abi.F_P]
+    L.tfg_set_deterministic.argtypes = [E, C.c_int]
+    abi.declare_server_api(L)
     _lib = L
     return L

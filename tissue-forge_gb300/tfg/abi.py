@@ -44,6 +44,7 @@ BOUNDARY_PERIODIC = 1 << 1
 BOUNDARY_FREESLIP = 1 << 2
 BOUNDARY_POTENTIAL = 1 << 3
 BOUNDARY_NO_SLIP = 1 << 4
+BOUNDARY_RESETTING = 1 << 5
 
 NEWTONIAN = 0
 OVERDAMPED = 1
@@ -150,3 +151,53 @@ def declare_potential_api(lib):
     lib.tfg_potential_free.argtypes = [P_POT]
     lib.tfg_potential_free.restype = None
     lib.tfg_potential_eval.argtypes = [P_POT, C.c_float, C.c_float, C.c_float, F_P, F_P]
+
+
+# ---- serving (tfg_server_*, tfg_request_*) ----
+SERVER_LEAST_WORK = 0
+SERVER_FIFO = 1
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
+class ServerDesc(C.Structure):
+    _fields_ = [("device", C.c_int32), ("quantum", C.c_int32), ("budget_bytes", C.c_int64),
+                ("max_particles", C.c_int64), ("policy", C.c_int32), ("discard_results", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("queued", C.c_int64), ("running", C.c_int64), ("particles_in_flight", C.c_int64),
+                ("bytes_in_flight", C.c_int64), ("max_concurrent", C.c_int64), ("chunks", C.c_int64)]
+
+
+def declare_server_api(lib):
+    """Prototypes of the serving entry points (the product library, or a test build of the
+    same server code over a stand-in batch)."""
+    S = R = C.c_void_p
+    i64p = C.POINTER(C.c_int64)
+    ip = C.POINTER(C.c_int)
+    lib.tfg_server_create.argtypes = [C.POINTER(ServerDesc), C.POINTER(S)]
+    lib.tfg_server_destroy.argtypes = [S]
+    lib.tfg_server_last_error.argtypes = [S]
+    lib.tfg_server_last_error.restype = C.c_char_p
+    lib.tfg_request_create.argtypes = [C.POINTER(EngineDesc), C.c_int, C.c_int, C.c_int, C.POINTER(R)]
+    lib.tfg_request_free.argtypes = [R]
+    lib.tfg_request_set_type.argtypes = [R, C.c_int, C.c_int, C.c_float]
+    lib.tfg_request_set_potential.argtypes = [R, C.c_int, C.c_int, P_POT]
+    lib.tfg_request_add_flux.argtypes = [R, C.c_int, C.c_int, C.POINTER(Flux)]
+    lib.tfg_request_set_species_flags.argtypes = [R, C.c_int, U_P]
+    lib.tfg_request_set_random_force.argtypes = [R, C.c_int, C.c_float, C.c_float, C.c_int]
+    lib.tfg_request_set_species_reset.argtypes = [R, C.c_int, F_P]
+    lib.tfg_request_set_boundary.argtypes = [R, C.c_int, C.POINTER(Boundary)]
+    lib.tfg_request_set_boundary_potential.argtypes = [R, C.c_int, C.c_int, P_POT]
+    lib.tfg_request_set_bonded_potential.argtypes = [R, C.c_int, P_POT]
+    lib.tfg_request_load_particles.argtypes = [R, C.c_int, F_P, F_P, I_P, F_P, F_P, U_P, F_P, F_P]
+    lib.tfg_request_load_bonds.argtypes = [R, C.c_int, I_P, I_P, I_P]
+    lib.tfg_request_load_angles.argtypes = [R, C.c_int, I_P, I_P, I_P, I_P]
+    lib.tfg_server_submit.argtypes = [S, R, i64p]
+    lib.tfg_server_poll.argtypes = [S, C.c_int, ip]
+    lib.tfg_server_take_finished.argtypes = [S, i64p, C.c_int, ip]
+    lib.tfg_server_request_info.argtypes = [S, C.c_int64, ip, ip, C.POINTER(C.c_double)]
+    lib.tfg_server_result.argtypes = [S, C.c_int64, ip, F_P, F_P, F_P, C.POINTER(Reductions)]
+    lib.tfg_server_release.argtypes = [S, C.c_int64]
+    lib.tfg_server_get_stats.argtypes = [S, C.POINTER(ServerStats)]

@@ -78,6 +78,7 @@ class Workload:
     angle_slot: Optional[np.ndarray] = None
     type_forces: list = field(default_factory=list)  # (type, mean, std, duration_steps)
     flags_particles: Optional[np.ndarray] = None      # per-particle flags (frozen axes)
+    species_reset: Optional[list] = None              # species values after a RESETTING wall
     force_i: Optional[np.ndarray] = None              # (n,3) external force per particle
     max_dist_fraction: float = 0.05                  # particle_max_dist_fraction
 

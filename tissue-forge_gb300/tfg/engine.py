@@ -77,6 +77,10 @@ class Engine:
         a = np.ascontiguousarray(flags, np.uint32)
         self._chk(self.L.tfg_set_species_flags(self.h, len(a), _up(a)), "set_species_flags")
 
+    def set_species_reset(self, values):
+        a = np.ascontiguousarray(values, np.float32)
+        self._chk(self.L.tfg_set_species_reset(self.h, len(a), _fp(a)), "set_species_reset")
+
     def set_random_force(self, t, mean, std, duration_steps):
         self._chk(self.L.tfg_set_random_force(self.h, t, mean, std, duration_steps), "set_random_force")
 
@@ -148,6 +152,15 @@ class Engine:
     def set_split(self, split):
         self._chk(self.L.tfg_set_split(self.h, split), "set_split")
 
+    def tuning(self):
+        """(split, warps per CTA, grab) the pair pass runs with (tfg_get_tuning)."""
+        v = [C.c_int() for _ in range(3)]
+        self._chk(self.L.tfg_get_tuning(self.h, *[C.byref(x) for x in v]), "get_tuning")
+        return tuple(int(x.value) for x in v)
+
+    def set_tuning(self, split, warps=8, grab=1):
+        self._chk(self.L.tfg_set_tuning(self.h, split, warps, grab), "set_tuning")
+
     def set_stream(self, stream_ptr):
         """Order the engine's work on the caller's CUDA stream (cudaStream_t as int)."""
         self._chk(self.L.tfg_engine_set_stream(self.h, C.c_void_p(stream_ptr)), "set_stream")
@@ -183,6 +196,32 @@ class Engine:
 
     def set_pair_lists(self, enable):
         self._chk(self.L.tfg_set_pair_lists(self.h, 1 if enable else 0), "set_pair_lists")
+
+    def pair_list(self):
+        """(n_pairs, 2) int32 array of the interacting pairs (lower id, higher id), sorted,
+        from the pair pass's own kernels (tfg_pair_list)."""
+        n = C.c_int64()
+        self._chk(self.L.tfg_pair_list(self.h, 0, None, C.byref(n)), "pair_list")
+        out = np.zeros((max(int(n.value), 1), 2), np.int32)
+        self._chk(self.L.tfg_pair_list(self.h, int(n.value), _ip(out), C.byref(n)), "pair_list")
+        out = out[: int(n.value)]
+        return out[np.lexsort((out[:, 1], out[:, 0]))]
+
+    def set_deterministic(self, enable):
+        """Pair pass without atomics: every run gives the same bits (tfg_set_deterministic)."""
+        self._chk(self.L.tfg_set_deterministic(self.h, 1 if enable else 0), "set_deterministic")
+
+    def resume(self, steps, q=None):
+        """After load_binned: restore the engine time and the pending flux increments of a
+        simulation saved mid-run (tfg_batch_resume on simulation 0)."""
+        q = _conv(q, np.float32)
+        self._chk(self.L.tfg_batch_resume(self.h, 0, int(steps), _fp(q)), "resume")
+
+    def status(self):
+        """0, or the first error (TFG_E_NAN / TFG_E_TOOFAST / TFG_E_RANGE) the simulation raised."""
+        st = C.c_int()
+        self._chk(self.L.tfg_batch_sim_status(self.h, 0, C.byref(st)), "batch_sim_status")
+        return int(st.value)
 
     def verlet(self):
         """(rebuilds so far, largest displacement since the last rebuild) in Verlet mode."""
@@ -275,6 +314,10 @@ class Sim:
         a = np.ascontiguousarray(flags, np.uint32)
         self._chk(self.L.tfg_batch_set_species_flags(self.b.h, self.sid, len(a), _up(a)), "batch_set_species_flags")
 
+    def set_species_reset(self, values):
+        a = np.ascontiguousarray(values, np.float32)
+        self._chk(self.L.tfg_batch_set_species_reset(self.b.h, self.sid, len(a), _fp(a)), "batch_set_species_reset")
+
     def set_random_force(self, t, mean, std, duration_steps):
         self._chk(self.L.tfg_batch_set_random_force(self.b.h, self.sid, t, mean, std, duration_steps),
                   "batch_set_random_force")
@@ -347,6 +390,17 @@ class Sim:
         self._chk(self.L.tfg_batch_get_verlet(self.b.h, self.sid, C.byref(nb), C.byref(m)), "batch_get_verlet")
         return int(nb.value), float(m.value)
 
+    def resume(self, steps, q=None):
+        """After load_binned: restore the engine time and pending flux increments."""
+        q = _conv(q, np.float32)
+        self._chk(self.L.tfg_batch_resume(self.b.h, self.sid, int(steps), _fp(q)), "batch_resume")
+
+    def status(self):
+        """0, or the first error (TFG_E_NAN / TFG_E_TOOFAST / TFG_E_RANGE) this simulation raised."""
+        st = C.c_int()
+        self._chk(self.L.tfg_batch_sim_status(self.b.h, self.sid, C.byref(st)), "batch_sim_status")
+        return int(st.value)
+
 
 def _potential(spec, cache, factory=None):
     make = factory or Potential.from_spec
@@ -384,6 +438,8 @@ def setup_model(eng, w, keep=None, pot_cache=None):
         eng.set_random_force(t, mean, std, dur)
     for (wall, kind, vel, restore, radius) in w.boundaries:
         eng.set_boundary(wall, kind, vel, restore, radius)
+    if w.species_reset is not None:
+        eng.set_species_reset(w.species_reset)
     for (wall, t, spec) in w.wall_pots:
         p = _potential(spec, pot_cache, factory)
         pots.append(p)
