@@ -357,6 +357,10 @@ def serve_sample(args, dev, count, rate=200.0, policy="sjf"):
                  keep_results=False, policy=policy)
     done = srv.run(reqs)
     s = summarize(done)
+    st = srv.stats()
+    s["host_s"] = {"admit": st["admit_s"], "launch": st["launch_s"], "retire": st["retire_s"],
+                   "note": "host time of the native server: recording requests into batches, starting "
+                           "chunks (arena re-layout after membership changes), retiring"}
     s.update({"policy": policy, "max_concurrent": srv.max_concurrent, "chunks": srv.chunks, "quantum": args.quantum,
               "max_particles_in_flight": args.serve_particles, "budget_bytes": 150 << 30,
               "rate_per_s": rate,

@@ -452,6 +452,10 @@ typedef struct tfg_server_stats {
     int64_t particles_in_flight, bytes_in_flight;
     int64_t max_concurrent;           /* largest number of simulations in flight so far */
     int64_t chunks;                   /* chunks launched over all batches */
+    /* host time spent, in seconds: admitting (recording requests into batches), starting
+     * chunks (tfg_batch_step: a re-layout of the arena after a membership change, then the
+     * graph launches), retiring (syncs, downloads, removals) */
+    double admit_s, launch_s, retire_s;
 } tfg_server_stats;
 
 TFG_API int tfg_server_create(const tfg_server_desc *desc, tfg_server **out);

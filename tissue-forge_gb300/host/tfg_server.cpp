@@ -221,8 +221,17 @@ bool fits(const tfg_server *S, const Record &R) {
 
 // Admit arrived requests in policy order while they fit (the first that does not fit waits
 // at the head, as a queue).
+int admit_inner(tfg_server *S);
+
 int admit(tfg_server *S) {
     if (S->arrived.empty()) return TFG_OK;
+    const auto t0 = Clock::now();
+    const int rc = admit_inner(S);
+    S->st.admit_s += std::chrono::duration<double>(Clock::now() - t0).count();
+    return rc;
+}
+
+int admit_inner(tfg_server *S) {
     if (S->desc.policy == TFG_SERVER_LEAST_WORK)
         std::stable_sort(S->arrived.begin(), S->arrived.end(), [&](int64_t a, int64_t b) {
             return S->records[a].particles * (double)S->records[a].req->nsteps <
@@ -309,6 +318,11 @@ int handle_error(tfg_server *S, Lane &L, int rc) {
 // The running chunk of lane L has completed on the device: account its steps, retire the
 // failed and the finished simulations.
 int complete_chunk(tfg_server *S, Lane &L) {
+    struct Timed {
+        tfg_server *S;
+        Clock::time_point t0;
+        ~Timed() { S->st.retire_s += std::chrono::duration<double>(Clock::now() - t0).count(); }
+    } timed{S, Clock::now()};
     const int rc = tfg_sync(L.batch);
     for (int sid : L.in_chunk) {
         auto it = L.active.find(sid);
@@ -343,7 +357,9 @@ int launch_idle(tfg_server *S) {
         L.in_chunk.clear();
         for (auto &a : L.active) L.in_chunk.insert(a.first);
         L.running = chunk;
+        const auto t0 = Clock::now();
         const int rs = tfg_batch_step(L.batch, chunk);
+        S->st.launch_s += std::chrono::duration<double>(Clock::now() - t0).count();
         S->st.chunks++;
         if (rs != TFG_OK) {
             // the chunk did not run as a whole: no steps are accounted, the failed leave

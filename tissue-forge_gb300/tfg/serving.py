@@ -185,7 +185,7 @@ class Server:
     def stats(self):
         st = abi.ServerStats()
         self.L.tfg_server_get_stats(self.h, C.byref(st))
-        return {k: int(getattr(st, k)) for k, _ in abi.ServerStats._fields_}
+        return {k: (float if t is C.c_double else int)(getattr(st, k)) for k, t in abi.ServerStats._fields_}
 
     @property
     def max_concurrent(self):
