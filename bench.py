@@ -392,7 +392,7 @@ def run_ensemble(args, rank, world, dev, dist):
         return b, sims
 
     b, sims = make_batch()
-    split = b.autotune()
+    split = tune(b, args)
     tuning = b.tuning()
     b.step(args.warmup)
     cnt0, _ = b.pair_signature()
@@ -434,7 +434,7 @@ def run_ensemble(args, rank, world, dev, dist):
         e = Engine(w.desc(device=dev))
         keep = setup_model(e, w, pot_cache=cache)
         e.set_stream(stream.cuda_stream)
-        e.autotune()
+        tune(e, args)
         e.step(3)
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a0.record(stream)
@@ -513,7 +513,7 @@ def run_ensemble(args, rank, world, dev, dist):
                              CPU_SAMPLE_ROUNDS, dt)}
     workloads = None
     if rank == 0 and args.sub_workloads:
-        workloads = {name: measure_workload(name, dev, stream, args.sub_steps, args.warmup)
+        workloads = {name: measure_workload(name, dev, stream, args.sub_steps, args.warmup, args)
                      for name in args.sub_workloads.split(",")}
     serving = serve_sample(args, dev, args.requests) if (rank == 0 and args.requests > 0) else None
     if serving is not None and args.sustained_requests > 0:
@@ -545,11 +545,20 @@ def run_ensemble(args, rank, world, dev, dist):
         print(json.dumps(line), flush=True)
 
 
+def tune(eng, args):
+    """Autotune the pair pass, or fix the tuple given with --tuning; returns the split."""
+    if args is not None and getattr(args, "tuning", ""):
+        split, warps, grab = (int(v) for v in args.tuning.split(","))
+        eng.set_tuning(split, warps, grab)
+        return split
+    return eng.autotune()
+
+
 def pair_kernel_name(split):
     return "k_pair_home" if split == 32 else "k_pair_tile (split %d)" % split
 
 
-def measure_workload(name, dev, stream, steps, warmup):
+def measure_workload(name, dev, stream, steps, warmup, args=None):
     """One single-simulation workload at its configured size on the plain path: particle-
     steps/s over `steps` steps with the L2 flushed before each, the pair kernel's time from
     stamped steps, and its FP32 roofline fraction (algorithmic flops of the interacting pairs)."""
@@ -565,7 +574,7 @@ def measure_workload(name, dev, stream, steps, warmup):
         eng.step(w.relax_steps)
         for t in range(w.max_type):
             eng.set_type(t, w.dynamics[t], w.mass[t])
-    split = eng.autotune()
+    split = tune(eng, args)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     value = timed_rate(eng, w.n, steps, warmup, flush, stream)
     cnt, _ = eng.pair_signature()
@@ -623,7 +632,7 @@ def run_single(args, rank, world, dev, dist):
         eng.step(w.relax_steps)
         for t in range(w.max_type):
             eng.set_type(t, w.dynamics[t], w.mass[t])
-    split = eng.autotune()
+    split = tune(eng, args)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     for _ in range(args.warmup):
         eng.step(1, sync=False)
@@ -673,7 +682,7 @@ def run_single(args, rank, world, dev, dist):
     e2e_eng = Engine(w.desc(device=dev))
     keep2 = setup_model(e2e_eng, w)
     e2e_eng.set_stream(stream.cuda_stream)
-    e2e_eng.set_split(split)
+    e2e_eng.set_tuning(*eng.tuning())
     ns = w.nr_species
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -770,6 +779,7 @@ def main():
     ap.add_argument("--sub-workloads", default="bonded_fluid,dpd_droplets",
                     help="single-simulation workloads measured beside the ensemble (comma list; empty: none)")
     ap.add_argument("--sub-steps", type=int, default=40, help="timed steps of each of those workloads")
+    ap.add_argument("--tuning", default="", help="fix the pair pass's tuple 'split,warps,grab' instead of autotuning")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 

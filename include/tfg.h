@@ -245,6 +245,14 @@ TFG_API int tfg_set_species_flags(tfg_engine *eng, int nr, const uint32_t *flags
 /* Species values a particle takes when it crosses a RESETTING boundary: nr values, one per
  * species index (default 0). */
 TFG_API int tfg_set_species_reset(tfg_engine *eng, int nr, const float *values);
+/* Stop the simulation when its clock (the step count, as tfg_get_reductions reports it)
+ * reaches `step`; -1 (the default) runs on.  The step calls of a stopped simulation leave
+ * it exactly as it is: positions, velocities, species, clock and the totals of its last
+ * step.  Raising the stop later lets it continue as if it had not paused.  This lets a
+ * batch step past the end of some of its members (tfg_batch_set_stop), which the serving
+ * loop uses to run whole chunks.  The reference has no counterpart: Universe::step runs
+ * one universe until its caller stops calling (tfUniverse.cpp). */
+TFG_API int tfg_set_stop(tfg_engine *eng, int64_t step);
 /* Gaussian single-body force per type (Force::random, tfForce.cpp:111-245): redraw
  * when (time + id) % duration_steps == 0; std <= 0 disables. */
 TFG_API int tfg_set_random_force(tfg_engine *eng, int type, float mean, float std, int duration_steps);
@@ -372,6 +380,7 @@ TFG_API int tfg_batch_set_potential(tfg_engine *eng, int sim, int ti, int tj, co
 TFG_API int tfg_batch_add_flux(tfg_engine *eng, int sim, int ti, int tj, const tfg_flux *flux);
 TFG_API int tfg_batch_set_species_flags(tfg_engine *eng, int sim, int nr, const uint32_t *flags);
 TFG_API int tfg_batch_set_species_reset(tfg_engine *eng, int sim, int nr, const float *values);
+TFG_API int tfg_batch_set_stop(tfg_engine *eng, int sim, int64_t step);
 TFG_API int tfg_batch_set_random_force(tfg_engine *eng, int sim, int type, float mean, float std,
                                        int duration_steps);
 TFG_API int tfg_batch_load_particles(tfg_engine *eng, int sim, int n, const float *x, const float *v,

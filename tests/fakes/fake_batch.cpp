@@ -3,11 +3,13 @@
 // server's admission, chunking and retirement logic is tested without a GPU.
 //
 // A simulation here is a particle count and a step counter.  A step advances every live
-// simulation; a simulation loaded with a non-finite coordinate fails at its first step
-// with TFG_E_NAN (reported by the next tfg_sync, as the device engine reports it).  A chunk
+// simulation that has not reached its stop (tfg_batch_set_stop); a simulation loaded with
+// a non-finite coordinate fails at its first step with TFG_E_NAN (reported by the next
+// tfg_sync, as the device engine reports it).  A chunk
 // stays "in flight" for a few tfg_query calls, so that requests arrive while it runs.
 // Downloads return the step count in every coordinate, so a test can check that each
 // request ran exactly its step count.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -18,11 +20,11 @@
 namespace {
 struct FakeSim {
     int n = 0;
-    long long steps = 0;
+    long long steps = 0, stop_at = -1;
     bool poison = false;
     int status = TFG_OK;
 };
-int g_max_chunk = 0, g_min_chunk = 1 << 30, g_max_live = 0, g_chunks = 0;
+int g_max_chunk = 0, g_min_chunk = 1 << 30, g_max_live = 0, g_chunks = 0, g_masked = 0;
 }  // namespace
 
 struct tfg_engine {
@@ -35,11 +37,15 @@ struct tfg_engine {
 
 extern "C" {
 
-TFG_API int tfg_fake_log(int *max_chunk, int *min_chunk, int *max_live, int *chunks) {
+// Chunk statistics since the last call; `masked` counts the simulation-steps that chunks
+// ran past a member's stop.
+TFG_API int tfg_fake_log(int *max_chunk, int *min_chunk, int *max_live, int *chunks, int *masked) {
     *max_chunk = g_max_chunk;
     *min_chunk = g_min_chunk;
     *max_live = g_max_live;
     *chunks = g_chunks;
+    *masked = g_masked;
+    g_masked = 0;
     g_max_chunk = 0;
     g_min_chunk = 1 << 30;
     g_max_live = 0;
@@ -73,6 +79,12 @@ TFG_API int tfg_batch_add_flux(tfg_engine *, int, int, int, const tfg_flux *) { 
 TFG_API int tfg_batch_set_species_flags(tfg_engine *, int, int, const uint32_t *) { return TFG_OK; }
 TFG_API int tfg_batch_set_random_force(tfg_engine *, int, int, float, float, int) { return TFG_OK; }
 TFG_API int tfg_batch_set_species_reset(tfg_engine *, int, int, const float *) { return TFG_OK; }
+TFG_API int tfg_batch_set_stop(tfg_engine *e, int sim, int64_t step) {
+    auto it = e->sims.find(sim);
+    if (it == e->sims.end() || step < -1) return TFG_E_INVAL;
+    it->second.stop_at = step;
+    return TFG_OK;
+}
 TFG_API int tfg_batch_set_boundary(tfg_engine *, int, int, const tfg_boundary *) { return TFG_OK; }
 TFG_API int tfg_batch_set_boundary_potential(tfg_engine *, int, int, int, const tfg_potential *) { return TFG_OK; }
 TFG_API int tfg_batch_load_particles(tfg_engine *e, int sim, int n, const float *x, const float *, const int32_t *,
@@ -99,9 +111,12 @@ TFG_API int tfg_batch_step(tfg_engine *e, int nsteps) {
     int live = 0;
     for (auto &kv : e->sims) {
         FakeSim &s = kv.second;
-        s.steps += nsteps;
+        long long k = nsteps;
+        if (s.stop_at >= 0) k = std::max(0LL, std::min(k, s.stop_at - s.steps));
+        g_masked += (int)(nsteps - k);
+        s.steps += k;
         live++;
-        if (s.poison && s.status == TFG_OK) {
+        if (k > 0 && s.poison && s.status == TFG_OK) {
             s.status = TFG_E_NAN;
             e->pending = TFG_E_NAN;
         }

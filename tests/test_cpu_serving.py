@@ -3,10 +3,10 @@
 The server's own code is compiled with a stand-in for the batch C ABI
 (tests/fakes/fake_batch.cpp: a simulation is a particle count and a step counter) into a
 test library, and driven through the Python client exactly as on the GPU.  Checked here:
-every request runs exactly its step count, chunks never exceed the quantum and are cut at
-the earliest finishing simulation, the particle cap and the byte budget hold, least-work-
-first and first-come-first-served admission orders, and a request whose particles fail is
-retired with its status while the others finish."""
+every request runs exactly its step count, chunks never exceed the quantum and run whole
+(members that finish inside a chunk stop themselves: tfg_batch_set_stop), the particle cap
+and the byte budget hold, least-work-first and first-come-first-served admission orders,
+and a request whose particles fail is retired with its status while the others finish."""
 import ctypes as C
 import os
 import subprocess
@@ -32,14 +32,14 @@ def fake():
                                "-I" + os.path.join(ROOT, "include"), "-o", OUT] + srcs)
     L = C.CDLL(OUT)
     abi.declare_server_api(L)
-    L.tfg_fake_log.argtypes = [C.POINTER(C.c_int)] * 4
+    L.tfg_fake_log.argtypes = [C.POINTER(C.c_int)] * 5
     return L
 
 
 def _log(L):
-    v = [C.c_int() for _ in range(4)]
+    v = [C.c_int() for _ in range(5)]
     L.tfg_fake_log(*[C.byref(x) for x in v])
-    return dict(zip(("max_chunk", "min_chunk", "max_live", "chunks"), (x.value for x in v)))
+    return dict(zip(("max_chunk", "min_chunk", "max_live", "chunks", "masked"), (x.value for x in v)))
 
 
 def _reqs():
@@ -62,6 +62,9 @@ def test_every_request_runs_exactly_its_steps(fake):
         assert r.t_admit >= r.t_arrival and r.t_done >= r.t_admit
     log = _log(fake)
     assert 1 <= log["min_chunk"] and log["max_chunk"] <= 16
+    # members finishing inside a chunk were stopped there (masked steps) instead of the
+    # chunk being cut for them
+    assert log["masked"] > 0 and log["max_chunk"] == 16
     assert srv.max_concurrent >= 2 and log["max_live"] >= 2
     st = srv.stats()
     assert st["completed"] == 6 and st["particles_in_flight"] == 0 and st["bytes_in_flight"] == 0

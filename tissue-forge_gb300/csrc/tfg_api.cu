@@ -301,6 +301,8 @@ TFG_API int tfg_set_species_reset(tfg_engine *eng, int nr, const float *values) 
 TFG_API int tfg_batch_set_species_reset(tfg_engine *eng, int sim, int nr, const float *values) {
     return set_species_reset(eng, sim, nr, values);
 }
+TFG_API int tfg_set_stop(tfg_engine *eng, int64_t step) { return set_stop_sim(eng, 0, step); }
+TFG_API int tfg_batch_set_stop(tfg_engine *eng, int sim, int64_t step) { return set_stop_sim(eng, sim, step); }
 TFG_API int tfg_set_random_force(tfg_engine *eng, int type, float mean, float std_, int duration_steps) {
     return set_random_force(eng, 0, type, mean, std_, duration_steps);
 }
@@ -414,9 +416,8 @@ TFG_API int tfg_force_only(tfg_engine *eng, int with_bonded) {
     if (rc) return rc;
     if (eng->split == 0 && (rc = autotune(eng))) return rc;
     cudaStream_t s = eng->stream;
-    for (int k : eng->order) eng->sims[k].time += 1;
-    launch_tick((int)eng->order.size(), eng->sims_dev, s);
-    CKE(cudaMemsetAsync(eng->red, 0, sizeof(double) * std::max<size_t>(eng->order.size(), 1) * RED_COUNT, s));
+    advance_clocks(eng);
+    launch_tick((int)eng->order.size(), eng->sims_dev, eng->red, s);
     rc = bin(eng, 1);
     if (rc) return rc;
     return force_pass(eng, with_bonded != 0, false);

@@ -90,6 +90,11 @@ struct SimParams {
     float wall_radius[6];
     int32_t wpot_base;       // (wall 0, type 0) in the wall-potential array; walls x types
     float species_reset[kMaxSpecies];  // species values after crossing a RESETTING wall
+    // A simulation may be told to stop at an engine time: k_tick sets `stopped` once time has
+    // reached stop_at, and every kernel of the step then leaves the simulation (and its
+    // totals) alone, so a batch can step on while some members are already done.
+    int64_t stop_at;         // -1: no stop
+    int32_t stopped;         // device: this step does not advance the simulation
     // Verlet mode (TFG_ENGINE_VERLET; engine_verlet_update, tfEngine.cpp:214-354).  The
     // device fields are written by k_tick and k_advance; the host writes 2 to
     // verlet_rebuild to force a rebuild at the next step.

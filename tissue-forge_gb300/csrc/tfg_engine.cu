@@ -636,6 +636,7 @@ int add_sim(tfg_engine *eng, const tfg_engine_desc *d, int *out) {
     // cutoff + skin at the rebuild; the margin covers the FP32 rounding of r2
     P.rlist2 = (P.cutoff + P.skin) * (P.cutoff + P.skin) * 1.0001f;
     P.verlet_rebuild = 2;
+    P.stop_at = -1;
     S.maxc = std::max(P.cdim[0], std::max(P.cdim[1], P.cdim[2]));
     S.orig.assign((size_t)3 * S.maxc, 0.f);
     for (int k = 0; k < 3; k++)
@@ -939,8 +940,7 @@ int flux_substeps(tfg_engine *eng) {
 int enqueue_step(tfg_engine *eng, bool advance, bool timed) {
     cudaStream_t s = eng->stream;
     const int nsims = (int)eng->order.size();
-    launch_tick(nsims, eng->sims_dev, s);
-    CK(cudaMemsetAsync(eng->red, 0, sizeof(double) * std::max(nsims, 1) * RED_COUNT, s));
+    launch_tick(nsims, eng->sims_dev, eng->red, s);   // also clears the advancing simulations' totals
     if (timed) launch_stamp(eng->stamps, 0, s);
     int rc = bin(eng, 1);
     if (rc) return rc;
@@ -955,9 +955,33 @@ int enqueue_step(tfg_engine *eng, bool advance, bool timed) {
     return check_launch(eng);
 }
 
+void advance_clocks(tfg_engine *eng) {
+    for (int k : eng->order) {
+        SimHost &S = eng->sims[k];
+        if (S.P.stop_at < 0 || S.time < S.P.stop_at) S.time += 1;
+    }
+}
+
 int one_step(tfg_engine *eng, bool advance, bool timed) {
-    for (int k : eng->order) eng->sims[k].time += 1;
+    advance_clocks(eng);
     return enqueue_step(eng, advance, timed);
+}
+
+// Stop simulation `sim` once its clock reaches `step` (-1: run on).  A simulation in the
+// arena gets the new value in its device parameters at once, in stream order; one not yet
+// laid out takes it with the next re-layout.
+int set_stop_sim(tfg_engine *eng, int sim, int64_t step) {
+    int rc = sim_check(eng, sim);
+    if (rc) return rc;
+    if (step < -1) return fail(eng, TFG_E_INVAL, "stop step must be -1 or at least 0");
+    SimHost &S = eng->sims[sim];
+    S.P.stop_at = step;
+    if (S.in_arena && !S.pending && eng->sims_dev) {
+        const size_t q = (size_t)S.P.red_base / RED_COUNT;
+        CK(cudaMemcpyAsync(reinterpret_cast<char *>(eng->sims_dev + q) + offsetof(SimParams, stop_at), &S.P.stop_at,
+                           sizeof(int64_t), cudaMemcpyHostToDevice, eng->stream));
+    }
+    return TFG_OK;
 }
 
 void drop_graphs(tfg_engine *eng) {
@@ -995,7 +1019,7 @@ int graph_step(tfg_engine *eng) {
     }
     CK(cudaGraphLaunch(eng->graph[p], eng->stream));
     eng->cur = eng->graph_next[p];
-    for (int k : eng->order) eng->sims[k].time += 1;
+    advance_clocks(eng);
     return TFG_OK;
 }
 

@@ -164,6 +164,8 @@ int commit(tfg_engine *eng);                    // re-lay the arena out and uplo
 int bin(tfg_engine *eng, int shuffle);
 int force_pass(tfg_engine *eng, bool bonded, bool timed);
 int one_step(tfg_engine *eng, bool advance, bool timed);
+void advance_clocks(tfg_engine *eng);           // host clocks, by k_tick's rule (stops included)
+int set_stop_sim(tfg_engine *eng, int sim, int64_t step);
 int enqueue_step(tfg_engine *eng, bool advance, bool timed);
 int flux_substeps(tfg_engine *eng);  // one_step without the host clock
 int graph_step(tfg_engine *eng);                // one step replayed from a captured graph

@@ -107,11 +107,21 @@ __global__ void k_stamp(unsigned long long *t, int k) {
 // time += 1 (engine_step, tfEngine.cpp:1387) and, in Verlet mode, the rebuild decision of
 // engine_verlet_update (tfEngine.cpp:234-290): rebuild when 2 * maxdx > skin, maxdx being
 // the largest displacement since the last rebuild, measured after the previous advance.
-__global__ void k_tick(int nsims, SimParams *sims) {
+// One step's start for every simulation: stop it if it has reached its stop time, else
+// advance its clock and clear its FP64 totals (a stopped simulation keeps the totals of its
+// last step).
+__global__ void k_tick(int nsims, SimParams *sims, double *red) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nsims) return;
     SimParams &P = sims[k];
+    if (P.stop_at >= 0 && P.time >= P.stop_at) {
+        P.stopped = 1;
+        if (P.verlet_rebuild == 1) P.verlet_rebuild = 0;
+        return;
+    }
+    P.stopped = 0;
     P.time += 1;
+    for (int r = 0; r < RED_COUNT; r++) red[P.red_base + r] = 0.0;
     if (P.flags & TFG_ENGINE_VERLET) {
         int rb = P.verlet_rebuild == 2;
         float m = 0.f;
@@ -184,8 +194,9 @@ __global__ void k_bin_count(int n, const SimParams *sims, const int32_t *cell_si
     int c = cell[i];
     if (shuffle) {
         const SimParams &P = sims[cell_sim[c]];
-        // Verlet mode re-bins only on rebuild steps (engine_verlet_update -> engine_shuffle)
-        if ((P.flags & TFG_ENGINE_VERLET) && !P.verlet_rebuild) {
+        // Verlet mode re-bins only on rebuild steps (engine_verlet_update -> engine_shuffle);
+        // a stopped simulation stays as it is
+        if (P.stopped || ((P.flags & TFG_ENGINE_VERLET) && !P.verlet_rebuild)) {
             lidx[i] = atomicAdd(&count[c], 1);
             return;
         }
@@ -356,8 +367,9 @@ __global__ void k_bonds(int nb, const SimParams *sims, const int32_t *cell_sim, 
         const int2 bd = bonds[b];
         const PotDev &pot = bpots[bslot[b]];
         const int si = slot_of_id[bd.x], sj = slot_of_id[bd.y];
-        if (pot.kind == POT_TABLE && si >= 0 && sj >= 0) {
-            const SimParams &P = sims[cell_sim[cell[si]]];
+        const SimParams *Pp = (si >= 0) ? &sims[cell_sim[cell[si]]] : nullptr;
+        if (pot.kind == POT_TABLE && si >= 0 && sj >= 0 && !Pp->stopped) {
+            const SimParams &P = *Pp;
             rb = P.red_base;
             const float4 pi = pos[si], pj = pos[sj];
             int ai, bi, ci, aj, bj, cj;
@@ -406,8 +418,9 @@ __global__ void k_angles(int na, const SimParams *sims, const int32_t *cell_sim,
         const int4 A = angles[q];
         const PotDev &pot = bpots[A.w];
         const int si = slot_of_id[A.x], sj = slot_of_id[A.y], sk = slot_of_id[A.z];
-        if (pot.kind == POT_TABLE && si >= 0 && sj >= 0 && sk >= 0) {
-            const SimParams &P = sims[cell_sim[cell[sj]]];
+        const SimParams *Pp = (sj >= 0) ? &sims[cell_sim[cell[sj]]] : nullptr;
+        if (pot.kind == POT_TABLE && si >= 0 && sj >= 0 && sk >= 0 && !Pp->stopped) {
+            const SimParams &P = *Pp;
             rb = P.red_base;
             const float4 pi = pos[si], pj = pos[sj], pk = pos[sk];
             int li[3], lj[3], lk[3];
@@ -502,7 +515,7 @@ __global__ void k_advance(int n, int cap, int nspec, SimParams *sims, const int3
     int rb = -1;
     int vsim = -1;          // Verlet simulation of this particle
     uint32_t dx2 = 0u;      // its squared displacement (float bits)
-    if (i < n) {
+    if (i < n && !sims[cell_sim[cell[i]]].stopped) {
         const int c0 = cell[i];
         const SimParams &P = sims[cell_sim[c0]];
         rb = P.red_base;
@@ -648,7 +661,7 @@ __global__ void k_flux_integrate(int n, int cap, int nspec, int sub, const SimPa
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const SimParams &P = sims[cell_sim[cell[i]]];
-    if (sub >= P.nr_fluxsteps - 1) return;
+    if (P.stopped || sub >= P.nr_fluxsteps - 1) return;
     for (int s = 0; s < nspec; s++) {
         const float konst = (species_flags[P.spec_base + s] & 1u) ? 0.f : 1.f;
         const float q = sq[s * cap + i];
@@ -695,8 +708,8 @@ inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 void launch_stamp(unsigned long long *t, int k, cudaStream_t s) { k_stamp<<<1, 1, 0, s>>>(t, k); }
 
-void launch_tick(int nsims, SimParams *sims, cudaStream_t s) {
-    if (nsims > 0) k_tick<<<nblk(nsims, 128), 128, 0, s>>>(nsims, sims);
+void launch_tick(int nsims, SimParams *sims, double *red, cudaStream_t s) {
+    if (nsims > 0) k_tick<<<nblk(nsims, 128), 128, 0, s>>>(nsims, sims, red);
 }
 
 void launch_setpartp(int n, const float *xg, const SimParams &P, float3 lo, float3 hi, float3 org, float3 ih,

@@ -21,7 +21,7 @@ struct BinArgs {
     float4 *oldx;   // Verlet reference positions by slot (written on rebuild steps), or null
 };
 
-void launch_tick(int nsims, SimParams *sims, cudaStream_t s);
+void launch_tick(int nsims, SimParams *sims, double *red, cudaStream_t s);
 // One thread writes the GPU global timer (ns) into t[k]: phase boundaries of a step, valid
 // inside captured graphs (event timing is not).
 void launch_stamp(unsigned long long *t, int k, cudaStream_t s);

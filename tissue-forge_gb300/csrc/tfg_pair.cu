@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kPairThreads) k_pair_stencil(PairKernelArgs a)
     const SimParams &P = a.sims[a.cell_sim[ci]];
     red_base = P.red_base;
     // flux-only substep pass: only simulations with a substep of this number take part
-    if (!kFluxOnly || a.flux_sub < P.nr_fluxsteps - 1) {
+    if ((kSig || !P.stopped) && (!kFluxOnly || a.flux_sub < P.nr_fluxsteps - 1)) {
     int li, lj, lk;
     cell_loc(P, ci, li, lj, lk);
 

@@ -127,6 +127,7 @@ __global__ void __launch_bounds__(kHW * 32, 2) k_pair_home(HomeArgs T) {
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         if (nh == 0) continue;
         const SimParams &P = a.sims[a.cell_sim[home]];
+        if (!kSig && P.stopped) continue;
         if (!kSig && P.red_base != cur_rb) {
             flush_red_h(a.red, cur_rb, epot, vir, lane);
             cur_rb = P.red_base;

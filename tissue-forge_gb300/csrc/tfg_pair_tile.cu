@@ -402,6 +402,7 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         if (nh == 0) continue;
         const SimParams &P = a.sims[a.cell_sim[home]];
+        if (!kSig && P.stopped) continue;
         if (kFlux && a.flux_sub >= 0 && a.flux_sub >= P.nr_fluxsteps - 1) continue;
         if (!kSig && P.red_base != cur_rb) {
             flush_red(a.red, cur_rb, epot, vir, lane);
@@ -677,6 +678,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
         const int home = T.overflow_list[w];
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         const SimParams &P = a.sims[a.cell_sim[home]];
+        if (!kSig && P.stopped) continue;
         const bool flux_only = kFlux && a.flux_sub >= 0;
         if (flux_only && a.flux_sub >= P.nr_fluxsteps - 1) continue;
         int li, lj, lk;

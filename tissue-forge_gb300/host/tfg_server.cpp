@@ -247,6 +247,8 @@ int admit_inner(tfg_server *S) {
         if (rc) return rc;
         int sim = -1;
         rc = replay(L->batch, *R.req, &sim);
+        // the simulation stops itself at its step count, so chunks need not end there
+        if (rc == TFG_OK) rc = tfg_batch_set_stop(L->batch, sim, R.req->nsteps);
         if (rc) {
             if (sim >= 0) tfg_batch_remove_sim(L->batch, sim);
             S->last_error = std::string("request ") + std::to_string(id) + ": " + tfg_last_error(L->batch);
@@ -338,16 +340,20 @@ int complete_chunk(tfg_server *S, Lane &L) {
     return done + (int)fin.size();
 }
 
-// Start the next chunk on every idle batch with simulations: the quantum, cut at the
-// nearest finishing simulation.  Returns the requests retired on the way (zero-step
-// requests, or a chunk that failed to start).
+// Start the next chunk on every idle batch with simulations: the quantum, or the longest
+// remaining step count when that is shorter.  Members that reach their step count inside
+// the chunk stop on the device (tfg_batch_set_stop) and wait there until the chunk ends,
+// so a chunk is not cut short and the batch is re-laid out once per chunk at most.
+// Returns the requests retired on the way (zero-step requests, or a chunk that failed to
+// start).
 int launch_idle(tfg_server *S) {
     int done = 0;
     for (auto &kv : S->lanes) {
         Lane &L = kv.second;
         if (L.running || L.active.empty()) continue;
-        int chunk = S->desc.quantum;
-        for (auto &a : L.active) chunk = std::min(chunk, a.second.remaining);
+        int longest = 0;
+        for (auto &a : L.active) longest = std::max(longest, a.second.remaining);
+        const int chunk = std::min(S->desc.quantum, longest);
         if (chunk <= 0) {   // zero-step requests finish at once
             L.running = 0;
             L.in_chunk.clear();

@@ -39,6 +39,8 @@ def lib():
     L.tfg_set_species_flags.argtypes = [E, C.c_int, abi.U_P]
     L.tfg_set_species_reset.argtypes = [E, C.c_int, abi.F_P]
     L.tfg_batch_set_species_reset.argtypes = [E, C.c_int, C.c_int, abi.F_P]
+    L.tfg_set_stop.argtypes = [E, C.c_int64]
+    L.tfg_batch_set_stop.argtypes = [E, C.c_int, C.c_int64]
     L.tfg_set_random_force.argtypes = [E, C.c_int, C.c_float, C.c_float, C.c_int]
     L.tfg_load_particles.argtypes = [E, C.c_int, abi.F_P, abi.F_P, abi.I_P, abi.F_P, abi.F_P, abi.U_P, abi.F_P,
                                      abi.F_P]

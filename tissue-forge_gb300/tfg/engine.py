@@ -81,6 +81,10 @@ class Engine:
         a = np.ascontiguousarray(values, np.float32)
         self._chk(self.L.tfg_set_species_reset(self.h, len(a), _fp(a)), "set_species_reset")
 
+    def set_stop(self, step):
+        """Stop at clock `step` (-1: run on); later steps leave the simulation as it is."""
+        self._chk(self.L.tfg_set_stop(self.h, int(step)), "set_stop")
+
     def set_random_force(self, t, mean, std, duration_steps):
         self._chk(self.L.tfg_set_random_force(self.h, t, mean, std, duration_steps), "set_random_force")
 
@@ -317,6 +321,10 @@ class Sim:
     def set_species_reset(self, values):
         a = np.ascontiguousarray(values, np.float32)
         self._chk(self.L.tfg_batch_set_species_reset(self.b.h, self.sid, len(a), _fp(a)), "batch_set_species_reset")
+
+    def set_stop(self, step):
+        """Stop this member at clock `step` (-1: run on) while the batch steps on."""
+        self._chk(self.L.tfg_batch_set_stop(self.b.h, self.sid, int(step)), "batch_set_stop")
 
     def set_random_force(self, t, mean, std, duration_steps):
         self._chk(self.L.tfg_batch_set_random_force(self.b.h, self.sid, t, mean, std, duration_steps),
