@@ -52,6 +52,9 @@ WORKLOADS = {
                         "N log-uniform in [1000, 200000], steps U[100, 5000]", bytes_per_particle=64),
     "dpd_droplets": dict(desc="DPD droplets with Fickian flux: 100,000 particles, box 40, cutoff 1, "
                               "alpha 10 gamma 4.5 sigma 3, Fick k 0.5, dt 0.01", bytes_per_particle=88),
+    "dpd_droplets_species": dict(desc="the DPD droplets with three species, each diffusing by Fick (k 0.5, 0.2, "
+                                      "0.1 with decay 0.05): 100,000 particles, box 40, cutoff 1",
+                                 bytes_per_particle=104),
     "bonded_fluid": dict(desc="LJ 12-6 fluid in chains of 16 with harmonic bonds and angles: 2,000,000 particles "
                               "at density 0.85, cutoff 2.5, dt 0.002", bytes_per_particle=80),
     "cell_sorting": dict(desc="cell sorting: 4,000 particles, box 20, cutoff 3, shifted Morse, overdamped",
@@ -77,6 +80,8 @@ def make_workload(name, seed, n=None, relax=None):
             scale = (n / 100_000) ** (1.0 / 3.0)
             return configs.dpd_droplets(n=n, side=40.0 * scale, radius=12.0 * scale, seed=1 + seed)
         return configs.dpd_droplets(seed=1 + seed)
+    if name == "dpd_droplets_species":
+        return configs.dpd_droplets_species(seed=1 + seed)
     if name == "bonded_fluid":
         w = configs.bonded_fluid(n=n or 2_000_000, seed=2 + seed)
         if relax is not None:
@@ -341,15 +346,52 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def serve_sample(args, dev, count, rate=200.0, policy="sjf"):
+def batched_same_requests(reqs, dev, steps=30):
+    """The served sample's requests run without the serving loop: all resident at once, one
+    batch per model family (as the server's lanes, each on its own stream, both in flight
+    together), every simulation stepped `steps` steps.  Its particle-steps/s is what the GPU
+    gives this request mix when nothing arrives, finishes or is re-laid out; the served
+    throughput is stated against it."""
+    from tfg.engine import Batch, setup_model
+    cache, groups = {}, {}
+    for r in reqs:
+        groups.setdefault((r.workload.max_type, r.workload.nr_species), []).append(r.workload)
+    batches = []
+    for (mt, ns), ws in groups.items():
+        b = Batch(mt, ns, dev)
+        for w in ws:
+            s = b.add_sim(w.desc(device=dev))
+            b._keep.extend(setup_model(s, w, pot_cache=cache))
+        b.step(3)   # layout, autotune, graph capture
+        batches.append(b)
+    n = sum(r.workload.n for r in reqs)
+    t0 = time.perf_counter()
+    for b in batches:
+        b.step(steps, sync=False)
+    for b in batches:
+        b.sync()
+    dt = time.perf_counter() - t0
+    for b in batches:
+        b.close()
+    return {"particle_steps_per_s": n * steps / dt, "particles": n, "steps": steps, "batches": len(batches),
+            "how": "the same requests, all resident, one batch per model family, %d steps each, host clock "
+                   "around both batches" % steps}
+
+
+def serve_sample(args, dev, count, rate=200.0, policy="sjf", compare_batched=False):
     """A bounded sample of the served stream: the first `count` requests of the Poisson
     stream at `rate` requests/s, with their particles generated before the clock starts
-    (client-side data)."""
+    (client-side data); a stream of more than 1,000 requests generates each request's
+    particles when it arrives instead, inside the clock."""
     from tfg import configs
     from tfg.serving import Request, Server, summarize
     reqs = []
+    lazy = count > 1000   # a long stream builds each request when it arrives
     for r in configs.served_requests(count=count, rate=rate, seed=args.seed):
-        reqs.append(Request(len(reqs), r["t"] - 0.0, configs.request_workload(r), r["steps"]))
+        if lazy:
+            reqs.append(Request(len(reqs), r["t"], None, r["steps"], make=lambda r=r: configs.request_workload(r)))
+        else:
+            reqs.append(Request(len(reqs), r["t"], configs.request_workload(r), r["steps"]))
     t_first = reqs[0].t_arrival
     for r in reqs:
         r.t_arrival -= t_first
@@ -361,6 +403,9 @@ def serve_sample(args, dev, count, rate=200.0, policy="sjf"):
     s["host_s"] = {"admit": st["admit_s"], "launch": st["launch_s"], "retire": st["retire_s"],
                    "note": "host time of the native server: recording requests into batches, starting "
                            "chunks (arena re-layout after membership changes), retiring"}
+    if compare_batched:
+        s["batched_same_requests"] = batched_same_requests(reqs, dev)
+        s["served_over_batched"] = s["achieved_particle_steps_per_s"] / s["batched_same_requests"]["particle_steps_per_s"]
     s.update({"policy": policy, "max_concurrent": srv.max_concurrent, "chunks": srv.chunks, "quantum": args.quantum,
               "max_particles_in_flight": args.serve_particles, "budget_bytes": 150 << 30,
               "rate_per_s": rate,
@@ -515,7 +560,7 @@ def run_ensemble(args, rank, world, dev, dist):
     if rank == 0 and args.sub_workloads:
         workloads = {name: measure_workload(name, dev, stream, args.sub_steps, args.warmup, args)
                      for name in args.sub_workloads.split(",")}
-    serving = serve_sample(args, dev, args.requests) if (rank == 0 and args.requests > 0) else None
+    serving = serve_sample(args, dev, args.requests, compare_batched=True) if (rank == 0 and args.requests > 0) else None
     if serving is not None and args.sustained_requests > 0:
         # the same stream at an arrival rate the GPU sustains (about half its served capacity),
         # so the latencies show service time rather than backlog
@@ -548,8 +593,8 @@ def run_ensemble(args, rank, world, dev, dist):
 def tune(eng, args):
     """Autotune the pair pass, or fix the tuple given with --tuning; returns the split."""
     if args is not None and getattr(args, "tuning", ""):
-        split, warps, grab = (int(v) for v in args.tuning.split(","))
-        eng.set_tuning(split, warps, grab)
+        eng.set_tuning(*(int(v) for v in args.tuning.split(",")))
+        split = eng.tuning()[0]
         return split
     return eng.autotune()
 
@@ -776,7 +821,7 @@ def main():
     ap.add_argument("--serve-particles", type=int, default=2_000_000, help="particles in flight cap")
     ap.add_argument("--quantum", type=int, default=50, help="largest chunk of steps between admissions")
     ap.add_argument("--seed", type=int, default=4)
-    ap.add_argument("--sub-workloads", default="bonded_fluid,dpd_droplets",
+    ap.add_argument("--sub-workloads", default="bonded_fluid,dpd_droplets,dpd_droplets_species",
                     help="single-simulation workloads measured beside the ensemble (comma list; empty: none)")
     ap.add_argument("--sub-steps", type=int, default=40, help="timed steps of each of those workloads")
     ap.add_argument("--tuning", default="", help="fix the pair pass's tuple 'split,warps,grab' instead of autotuning")

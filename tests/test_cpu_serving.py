@@ -131,3 +131,23 @@ def test_failed_request_is_retired_alone(fake):
     assert st["failed"] == 1 and st["completed"] == 5
     s = summarize(done)
     assert s["failed"] == 1
+
+
+def test_lazily_built_requests(fake):
+    """Requests built when they arrive (Request(..., None, steps, make=...)) run like the
+    others; after submission the client keeps only their shape."""
+    built = []
+
+    def make(i, n):
+        def f():
+            built.append(i)
+            return configs.cell_sorting(n=n, side=12.0, seed=i)
+        return f
+
+    reqs = [Request(i, 0.0005 * i, None, 5 + i, make=make(i, 400 + 100 * i)) for i in range(4)]
+    srv = Server(max_particles=10 ** 9, quantum=4, lib=fake)
+    done = srv.run(reqs)
+    assert sorted(built) == [0, 1, 2, 3]
+    for r in done:
+        assert r.status == 0 and np.all(r.result["x"] == r.steps)
+        assert r.workload.n == 400 + 100 * r.rid and not hasattr(r.workload, "x")

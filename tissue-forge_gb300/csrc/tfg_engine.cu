@@ -897,7 +897,7 @@ const TilePlan &tile_plan(tfg_engine *eng, int split) {
 }
 
 // The tiled half-shell kernel handles at most one species; more go to the stencil kernel.
-bool use_tile(const tfg_engine *eng) { return !eng->deterministic && !(eng->has_flux && eng->nspec > 1); }
+bool use_tile(const tfg_engine *eng) { return !eng->deterministic; }
 
 int force_pass(tfg_engine *eng, bool bonded, bool timed) {
     cudaStream_t s = eng->stream;

@@ -113,7 +113,12 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
             term = __fmul_rn(term, term);
             const bool a_is_I = (ti == F.type_a);
             const bool b_is_K = (tk == F.type_b);
-            const float ssi = a_is_I ? S.sv[I] : S.sv[K], ssj = b_is_K ? S.sv[K] : S.sv[I];
+            // staged indices of the flux's "a" and "b" particles; one species is staged, more
+            // are read from the particle arrays and their increments added there directly
+            const int sa = a_is_I ? I : K, sb = b_is_K ? K : I;
+            const bool one = a.nspec == 1;
+            const size_t ga = (size_t)F.index_a * a.cap + S.gslot[sa], gb = (size_t)F.index_b * a.cap + S.gslot[sb];
+            const float ssi = one ? S.sv[sa] : a.sval[ga], ssj = one ? S.sv[sb] : a.sval[gb];
             float q = term;
             if (F.kind == TFG_FLUX_FICK) {
                 q = __fmul_rn(q, __fmul_rn(F.coef, __fsub_rn(ssi, ssj)));
@@ -125,8 +130,13 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
                 q = __fmul_rn(q, qq > 0.f ? qq : 0.f);
             }
             const float da = -q - F.half_decay * ssi, db = q - F.half_decay * ssj;
-            if (a_is_I) qI += da; else qK += da;
-            if (b_is_K) qK += db; else qI += db;
+            if (one) {
+                if (a_is_I) qI += da; else qK += da;
+                if (b_is_K) qK += db; else qI += db;
+            } else {
+                atomicAdd(&a.sq[ga], da);
+                atomicAdd(&a.sq[gb], db);
+            }
         }
     }
     if (flux_only) return;

@@ -167,6 +167,41 @@ def dpd_droplets(n=100_000, side=40.0, cutoff=1.0, radius=12.0, steps=1000, seed
     return w
 
 
+def dpd_droplets_species(n=100_000, side=40.0, cutoff=1.0, radius=12.0, steps=1000, seed=1):
+    """The DPD droplets with three species, each diffusing by Fick (the multi-species flux
+    path): the droplet marker of dpd_droplets (k 0.5), a second species from a uniform random
+    start (k 0.2) and a third from a uniform 0.25 with decay (k 0.1, decay 0.05).  All
+    particles have one type, so only symmetric fluxes are used: a flux whose two sides differ
+    (secrete, uptake, or two species indices) between particles of one type acts from the
+    pair's first particle to its second, and which is first depends on the order of the
+    particles in their cell."""
+    w = dpd_droplets(n=n, side=side, cutoff=cutoff, radius=radius, steps=steps, seed=seed)
+    rng = np.random.default_rng(np.random.PCG64(1500 + seed))
+    s = np.zeros((w.n, 3), np.float32)
+    s[:, 0] = w.species[:, 0]
+    s[:, 1] = rng.uniform(0.0, 1.0, size=w.n).astype(np.float32)
+    s[:, 2] = 0.25
+    w.species = s
+    w.nr_species = 3
+    w.name = "dpd_droplets_species"
+    w.fluxes = []
+    for kind, ia, ib, coef, decay, target in [(abi.FLUX_FICK, 0, 0, 0.5, 0.0, 0.0),
+                                              (abi.FLUX_FICK, 1, 1, 0.2, 0.0, 0.0),
+                                              (abi.FLUX_FICK, 2, 2, 0.1, 0.05, 0.0)]:
+        f = abi.Flux()
+        f.kind = kind
+        f.type_a = 0
+        f.type_b = 0
+        f.index_a = ia
+        f.index_b = ib
+        f.coef = coef
+        f.decay = decay
+        f.target = target
+        f.cutoff = cutoff
+        w.fluxes.append((0, 0, f))
+    return w
+
+
 def bonded_fluid(n=2_000_000, density=0.85, cutoff=2.5, chain=16, steps=500, relax_steps=50, seed=2):
     rng = np.random.default_rng(np.random.PCG64(2000 + seed))
     n = (n // chain) * chain

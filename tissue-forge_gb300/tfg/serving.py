@@ -6,10 +6,11 @@ of steps; its result is the final particle state.  The server itself is native: 
 one batch (a device arena, tfg_batch_*) per model family -- simulations of one batch share
 their type count and species count -- on its own CUDA stream, admits arrived requests under
 an HBM byte budget and a cap on particles in flight (least work, particles x steps, first;
-or first come, first served), advances every batch in chunks of at most `quantum` steps cut
-so that no simulation runs past its step count, and at each chunk boundary retires the
-finished simulations and admits waiting requests, which join without waiting for the batch
-to drain.  A simulation whose particles raise an error (non-finite position, a particle
+or first come, first served), advances every batch in chunks of at most `quantum` steps (a
+simulation that reaches its step count inside a chunk stops itself there and waits,
+unchanged, for the chunk to end), and at each chunk boundary retires the finished
+simulations and admits waiting requests, which join without waiting for the batch to
+drain.  A simulation whose particles raise an error (non-finite position, a particle
 faster than one cell per step) is retired as failed with that status while the rest of its
 batch continues.  This module builds each request through the C ABI (RequestBuilder has the
 engine-like method names, so engine.setup_model fills it), submits it at its arrival time and
@@ -40,13 +41,26 @@ def footprint(w):
     return w.n * _bytes_per_particle(w.nr_species) + int(np.prod(w.cells)) * 16 + nb * 12 + na * 16
 
 
-class Request:
-    __slots__ = ("rid", "t_arrival", "workload", "steps", "t_admit", "t_done", "result", "reductions", "status")
+class _Shape:
+    """What the client keeps of a lazily built request's workload once it is submitted."""
+    __slots__ = ("n", "nr_species", "name")
 
-    def __init__(self, rid, t_arrival, workload, steps):
+    def __init__(self, w):
+        self.n, self.nr_species, self.name = w.n, w.nr_species, w.name
+
+
+class Request:
+    """One simulation request.  `workload` is a configs.Workload, or None with `make` a
+    callable that builds it: such a request is built when it arrives, and after submission
+    the client keeps only its shape (the server holds the particle data)."""
+    __slots__ = ("rid", "t_arrival", "workload", "steps", "t_admit", "t_done", "result", "reductions", "status",
+                 "make")
+
+    def __init__(self, rid, t_arrival, workload, steps, make=None):
         self.rid = rid
         self.t_arrival = float(t_arrival)
         self.workload = workload
+        self.make = make
         self.steps = int(steps)
         self.t_admit = None
         self.t_done = None
@@ -196,6 +210,8 @@ class Server:
         return self.stats()["chunks"]
 
     def _submit(self, r, pot_cache):
+        if r.workload is None:
+            r.workload = r.make()
         if footprint(r.workload) > self.budget:
             raise ValueError("request %r does not fit the HBM budget" % r.rid)
         b = RequestBuilder(self.L, r.workload, r.steps)
@@ -211,6 +227,8 @@ class Server:
             raise RuntimeError("tfg_server_submit: %s (%s)" % (abi.STATUS_NAMES.get(rc, rc),
                                                               self.L.tfg_server_last_error(self.h).decode()))
         b.h = C.c_void_p()   # the server owns it now
+        if r.make is not None:
+            r.workload = _Shape(r.workload)
         return int(rid.value)
 
     def _collect(self, sid, r, now, t_submit):
@@ -241,7 +259,7 @@ class Server:
         filled in (result None for a failed request)."""
         pending = collections.deque(sorted(requests, key=lambda r: r.t_arrival))
         for r in pending:
-            if footprint(r.workload) > self.budget:
+            if r.workload is not None and footprint(r.workload) > self.budget:
                 raise ValueError("request %r does not fit the HBM budget" % r.rid)
         t0 = time.perf_counter()
         clock = clock or (lambda: time.perf_counter() - t0)
