@@ -401,11 +401,17 @@ def serve_sample(args, dev, count, rate=200.0, policy="sjf", compare_batched=Fal
     s = summarize(done)
     st = srv.stats()
     s["host_s"] = {"admit": st["admit_s"], "launch": st["launch_s"], "retire": st["retire_s"],
+                   "batch_busy": st["busy_s"], "batch_gap": st["gap_s"],
                    "note": "host time of the native server: recording requests into batches, starting "
-                           "chunks (arena re-layout after membership changes), retiring"}
+                           "chunks (arena re-layout after membership changes), retiring; batch_busy and "
+                           "batch_gap sum over the batches the time from a chunk's start to its observed "
+                           "completion and from there to the batch's next chunk"}
     if compare_batched:
         s["batched_same_requests"] = batched_same_requests(reqs, dev)
-        s["served_over_batched"] = s["achieved_particle_steps_per_s"] / s["batched_same_requests"]["particle_steps_per_s"]
+        ref = s["batched_same_requests"]["particle_steps_per_s"]
+        s["served_over_batched"] = s["achieved_particle_steps_per_s"] / ref
+        if s["backlogged_particle_steps_per_s"]:
+            s["backlogged_over_batched"] = s["backlogged_particle_steps_per_s"] / ref
     s.update({"policy": policy, "max_concurrent": srv.max_concurrent, "chunks": srv.chunks, "quantum": args.quantum,
               "max_particles_in_flight": args.serve_particles, "budget_bytes": 150 << 30,
               "rate_per_s": rate,

@@ -303,7 +303,9 @@ TFG_API int tfg_set_pair_lists(tfg_engine *eng, int enable);
  * cell: 1, 2, 7 or 14) and, for engines whose potentials are all tabulated (no DPD, no
  * fluxes, no Verlet pair lists), TFG_PAIR_HOME_OUTER: the kernel that takes home particles
  * one at a time against targets held in registers.  tfg_step and tfg_force_only run it on
- * their first call; tfg_set_split fixes the choice instead (TFG_PAIR_HOME_OUTER falls back
+ * their first call, and time the work splits again whenever the particle count has grown
+ * or shrunk more than 4x since (a batch that fills up or drains); tfg_set_split fixes the
+ * choice instead (TFG_PAIR_HOME_OUTER falls back
  * to split 1 while the engine is not eligible).  The reference selects CUDA
  * blocks/threads by hand (cuda::EngineConfig::setBlocks / setThreads,
  * source/cuda/tfEngineConfig.cpp:98-124). */
@@ -465,6 +467,10 @@ typedef struct tfg_server_stats {
      * chunks (tfg_batch_step: a re-layout of the arena after a membership change, then the
      * graph launches), retiring (syncs, downloads, removals) */
     double admit_s, launch_s, retire_s;
+    /* summed over the batches: wall time from starting a chunk to seeing it complete
+     * (busy_s), and from a chunk's completion to the start of the batch's next chunk while
+     * the batch still held simulations (gap_s: the host turn between chunks) */
+    double busy_s, gap_s;
 } tfg_server_stats;
 
 TFG_API int tfg_server_create(const tfg_server_desc *desc, tfg_server **out);

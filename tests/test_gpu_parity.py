@@ -10,7 +10,7 @@ import pytest
 import oracle as O
 from helpers import FORCE_RTOL, force_error, make_gpu, make_oracle, small_bonded, small_cell_sorting, small_dpd
 from tfg import abi, configs
-from tfg.engine import Engine, TfgError, setup_model
+from tfg.engine import Batch, Engine, TfgError, setup_model
 
 pytestmark = pytest.mark.gpu
 
@@ -251,3 +251,30 @@ def test_empty_and_ragged_cells():
         oc, oh = o.signature()
         assert np.array_equal(gc, oc) and np.array_equal(gh, oh)
         assert force_error(g.download()["f"], o.download()["f"], o.fmag()) < FORCE_RTOL
+
+
+def test_retune_after_growth_keeps_results():
+    """A batch tuned on one small member and then grown more than 4x re-times its work
+    split at the next step; the members still equal their alone runs."""
+    ws = [configs.cell_sorting(n=600, side=11.0, seed=71)] + \
+         [configs.cell_sorting(n=3000, side=18.0, seed=72 + k) for k in range(4)]
+    b = Batch(ws[0].max_type, ws[0].nr_species)
+    first = b.add_sim(ws[0].desc())
+    b._keep.extend(setup_model(first, ws[0]))
+    b.step(2)
+    t_small = b.tuning()
+    sims = [first]
+    for w in ws[1:]:
+        s = b.add_sim(w.desc())
+        b._keep.extend(setup_model(s, w))
+        sims.append(s)
+    b.step(3)
+    t_big = b.tuning()
+    assert t_big[0] in (1, 2, 7, 14, abi.PAIR_HOME_OUTER) and t_small[0] in (1, 2, 7, 14, abi.PAIR_HOME_OUTER)
+    for s, w, steps in zip(sims, ws, [5, 3, 3, 3, 3]):
+        g = make_gpu(w)
+        g.step(steps)
+        side = np.array(w.dim, np.float32)
+        d = s.download()["x"] - g.download()["x"]
+        d -= side * np.round(d / side)
+        assert np.max(np.abs(d)) < 1e-3

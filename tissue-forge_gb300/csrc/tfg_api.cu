@@ -376,6 +376,7 @@ TFG_API int tfg_set_split(tfg_engine *eng, int split) {
     if (!eng || !(split == 1 || split == 2 || split == 7 || split == 14 || split == TFG_PAIR_HOME_OUTER))
         return TFG_E_INVAL;
     eng->split = split;
+    eng->tune_auto = false;
     eng->gen++;
     return TFG_OK;
 }
@@ -385,7 +386,7 @@ TFG_API int tfg_step(tfg_engine *eng, int nsteps) {
     if (!any_particles(eng)) return fail(eng, TFG_E_STATE, "no particles loaded");
     int rc = commit(eng);
     if (rc) return rc;
-    if (eng->split == 0 && (rc = autotune(eng))) return rc;
+    if ((rc = tune_if_needed(eng))) return rc;
     return run_steps(eng, nsteps);
 }
 
@@ -414,7 +415,7 @@ TFG_API int tfg_force_only(tfg_engine *eng, int with_bonded) {
     if (!any_particles(eng)) return fail(eng, TFG_E_STATE, "no particles loaded");
     int rc = commit(eng);
     if (rc) return rc;
-    if (eng->split == 0 && (rc = autotune(eng))) return rc;
+    if ((rc = tune_if_needed(eng))) return rc;
     cudaStream_t s = eng->stream;
     advance_clocks(eng);
     launch_tick((int)eng->order.size(), eng->sims_dev, eng->red, s);
@@ -552,6 +553,7 @@ TFG_API int tfg_set_tuning(tfg_engine *eng, int split, int warps, int grab) {
     eng->split = split;
     eng->tune_warps = warps;
     eng->tune_grab = grab;
+    eng->tune_auto = false;
     eng->gen++;
     return TFG_OK;
 }

@@ -1050,9 +1050,19 @@ int run_steps(tfg_engine *eng, int nsteps) {
 // the current binned state.  Every trial re-initialises the forces with a non-shuffling
 // re-bin (idempotent on sorted data); the flux increments the trials add are saved and
 // restored, so the engine state is unchanged.
-int autotune(tfg_engine *eng) {
+int tune_if_needed(tfg_engine *eng) {
+    if (eng->split == 0) return autotune(eng);
+    // A batch whose population changed by more than 4x since the autotuner ran (a served
+    // batch that filled up or drained) re-times the work split, the knob that follows size.
+    if (eng->tune_auto && (eng->n > 4 * eng->tuned_n || 4 * eng->n < eng->tuned_n)) return autotune(eng, true);
+    return TFG_OK;
+}
+
+int autotune(tfg_engine *eng, bool splits_only) {
     if (!use_tile(eng) || eng->n == 0 || eng->lists_on) {
         eng->split = 1;
+        eng->tune_auto = true;
+        eng->tuned_n = eng->n;
         return TFG_OK;
     }
     cudaStream_t s = eng->stream;
@@ -1070,13 +1080,15 @@ int autotune(tfg_engine *eng) {
         for (int warps : {8, 4})
             for (int grab : {1, 2, 4}) {
                 if (warps == 4 && !table_only) continue;
+                // a re-tune keeps the CTA shape and grab and times the splits only
+                if (splits_only && (warps != eng->tune_warps || grab != eng->tune_grab)) continue;
                 TileTune t;
                 t.split = split;
                 t.warps = warps;
                 t.grab = grab;
                 cand.push_back(t);
             }
-    if (pair_home_eligible(a0)) {
+    if (!splits_only && pair_home_eligible(a0)) {
         TileTune t;
         t.split = TFG_PAIR_HOME_OUTER;
         cand.push_back(t);
@@ -1109,6 +1121,8 @@ int autotune(tfg_engine *eng) {
     eng->split = best_t.split;
     eng->tune_warps = best_t.warps;
     eng->tune_grab = best_t.grab;
+    eng->tune_auto = true;
+    eng->tuned_n = eng->n;
     eng->gen++;
     return check_launch(eng);
 }

@@ -119,6 +119,8 @@ struct tfg_engine {
     int max_fluxsteps = 1;           // largest nr_fluxsteps of a simulation with fluxes
     uint32_t flags_all = 0;          // TFG_ENGINE_NO_DENSITY only when every simulation sets it
     int split = 0;                   // tiled pair pass: warps per home cell (0 = not tuned)
+    bool tune_auto = false;          // the tuple is the autotuner's (not fixed by the caller)
+    int64_t tuned_n = 0;             // particles when the autotuner last ran
     int tune_warps = 8;              // tiled pair pass: warps per CTA (table variants: 8 or 4)
     int tune_grab = 1;               // tiled pair pass: work items per grab
     bool deterministic = false;      // pair pass without atomics (stencil kernel): reproducible bits
@@ -170,7 +172,8 @@ int enqueue_step(tfg_engine *eng, bool advance, bool timed);
 int flux_substeps(tfg_engine *eng);  // one_step without the host clock
 int graph_step(tfg_engine *eng);                // one step replayed from a captured graph
 int run_steps(tfg_engine *eng, int nsteps);     // nsteps steps, graphs where they apply
-int autotune(tfg_engine *eng);
+int autotune(tfg_engine *eng, bool splits_only = false);
+int tune_if_needed(tfg_engine *eng);   // first tuning, or a re-tune after the batch grew or shrank 4x
 inline TileTune tune_of(const tfg_engine *eng) {
     TileTune t;
     t.split = eng->split;

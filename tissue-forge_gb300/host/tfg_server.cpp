@@ -106,6 +106,9 @@ struct Lane {
     std::map<int, Active> active;     // by simulation id in the batch
     std::set<int> in_chunk;           // simulations stepping in the running chunk
     int running = 0;                  // steps of the running chunk (0: idle)
+    Clock::time_point t_launch{};     // start of the running chunk
+    Clock::time_point t_done{};       // completion of the last chunk, while simulations remain
+    bool waiting = false;             // t_done is set: the batch waits for its next chunk
 };
 
 }  // namespace
@@ -326,6 +329,8 @@ int complete_chunk(tfg_server *S, Lane &L) {
         ~Timed() { S->st.retire_s += std::chrono::duration<double>(Clock::now() - t0).count(); }
     } timed{S, Clock::now()};
     const int rc = tfg_sync(L.batch);
+    const auto t_end = Clock::now();
+    if (L.running) S->st.busy_s += std::chrono::duration<double>(t_end - L.t_launch).count();
     for (int sid : L.in_chunk) {
         auto it = L.active.find(sid);
         if (it != L.active.end()) it->second.remaining -= L.running;
@@ -337,6 +342,8 @@ int complete_chunk(tfg_server *S, Lane &L) {
     for (auto &kv : L.active)
         if (kv.second.remaining <= 0) fin.push_back(kv.first);
     for (int sid : fin) retire(S, L, sid, TFG_REQ_DONE, TFG_OK);
+    L.waiting = !L.active.empty();
+    L.t_done = t_end;
     return done + (int)fin.size();
 }
 
@@ -364,6 +371,9 @@ int launch_idle(tfg_server *S) {
         for (auto &a : L.active) L.in_chunk.insert(a.first);
         L.running = chunk;
         const auto t0 = Clock::now();
+        if (L.waiting) S->st.gap_s += std::chrono::duration<double>(t0 - L.t_done).count();
+        L.waiting = false;
+        L.t_launch = t0;
         const int rs = tfg_batch_step(L.batch, chunk);
         S->st.launch_s += std::chrono::duration<double>(Clock::now() - t0).count();
         S->st.chunks++;

@@ -168,7 +168,8 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
                 ("queued", C.c_int64), ("running", C.c_int64), ("particles_in_flight", C.c_int64),
                 ("bytes_in_flight", C.c_int64), ("max_concurrent", C.c_int64), ("chunks", C.c_int64),
-                ("admit_s", C.c_double), ("launch_s", C.c_double), ("retire_s", C.c_double)]
+                ("admit_s", C.c_double), ("launch_s", C.c_double), ("retire_s", C.c_double),
+                ("busy_s", C.c_double), ("gap_s", C.c_double)]
 
 
 def declare_server_api(lib):

@@ -302,6 +302,26 @@ class Server:
         return finished
 
 
+def backlogged_rate(reqs):
+    """Particle-steps per second while requests were waiting for admission: from the first
+    admission to the last, each finished request's particle-steps spread evenly over its
+    time in the server.  This is the served rate without the start of the run (filling the
+    server) and its drain (the last requests running with room to spare).  None when every
+    request was admitted at once."""
+    ok = [r for r in reqs if not r.status and r.t_admit is not None and r.t_done > r.t_admit]
+    if not ok:
+        return None
+    t0, t1 = min(r.t_admit for r in ok), max(r.t_admit for r in ok)
+    if t1 - t0 <= 0:
+        return None
+    acc = 0.0
+    for r in ok:
+        lo, hi = max(r.t_admit, t0), min(r.t_done, t1)
+        if hi > lo:
+            acc += r.workload.n * r.steps * (hi - lo) / (r.t_done - r.t_admit)
+    return acc / (t1 - t0)
+
+
 def summarize(reqs):
     """Throughput and latency figures of a served run (failed requests count in latency,
     not in the particle-steps)."""
@@ -311,6 +331,7 @@ def summarize(reqs):
     t_last = max(r.t_done for r in reqs)
     span_arrivals = max(r.t_arrival for r in reqs) - t_first
     return {
+        "backlogged_particle_steps_per_s": backlogged_rate(reqs),
         "requests": len(reqs),
         "failed": sum(1 for r in reqs if r.status),
         "particle_steps": work,
