@@ -10,12 +10,13 @@
 // task-partner of the home cell with the home as cell_i exactly when d is
 // lexicographically positive, space_getsid / space_init tfSpace.cpp:79-114, 893-1019).
 // The home cell and then each neighbour cell are staged into the warp's shared memory;
-// all 32 lanes test candidate pairs (r2 with the reference's unfused FP32 arithmetic, so
-// the pair set is bit-identical), hits go to a warp-private ring queue, and the queue is
-// evaluated 32 pairs at a time so the force arithmetic runs with full lanes.  Forces,
-// number densities and flux increments of both partners accumulate in shared memory and
-// each staged particle is flushed once to global memory with a vector atomic add.
-// Cells above the staging capacity are listed and handled by k_pair_overflow.
+// a neighbour particle is staged only if it lies within the cutoff of the box holding the
+// home particles.  All 32 lanes test candidate pairs (r2 with the reference's unfused FP32
+// arithmetic, so the pair set is bit-identical), hits go to a warp-private ring queue, and
+// the queue is evaluated 32 pairs at a time so the force arithmetic runs with full lanes.
+// Each evaluated pair adds the force, number density and flux increments of both partners
+// to the particle arrays with global vector atomics.  Cells above the staging capacity are
+// listed and handled by k_pair_overflow.
 #include <algorithm>
 
 #include "tfg_internal.h"
@@ -34,12 +35,13 @@ constexpr int kMaxSmemPots = 64;    // potential descriptors staged per CTA (all
 constexpr size_t kFourCtaBytes = 228 * 1024 / 4 - 1024;   // dynamic shared memory of a CTA, four per SM
 
 // One warp's staging area.  The DPD and flux variants (EXTRA) also stage each particle's
-// velocity, id, species value and flux increment, with fewer particles per warp, so that
-// every variant fits four CTAs per SM.
-template <int CAP, bool EXTRA> struct StagedT {
+// velocity, id and species value, with fewer particles per warp, so that every variant fits
+// four CTAs per SM.  Force variants add each pair's increments straight to the particle
+// arrays; only the signature variant (SIG) keeps per-particle sums in shared memory.
+template <int CAP, bool EXTRA, bool SIG> struct StagedT {
     static constexpr int cap = CAP;
     float4 pos[CAP];        // cell-relative position; w = type bits
-    float4 acc[CAP];        // fx, fy, fz, number density (signature: count, hash bits)
+    float4 acc[SIG ? CAP : 1];   // signature: partner count, id hash (bits)
     int32_t gslot[CAP];     // global slot of the staged particle
     float rad[CAP];         // radius
     float sh[27][3];        // shift of each task's partner cell (space_getsid)
@@ -47,7 +49,7 @@ template <int CAP, bool EXTRA> struct StagedT {
     float4 vel[EXTRA ? CAP : 1];
     int32_t id[EXTRA ? CAP : 1];
     float sv[EXTRA ? CAP : 1];   // species 0 value
-    float sq[EXTRA ? CAP : 1];   // species 0 flux increment
+    float4 box[2];          // box holding every home particle (lo, hi); lo.w: squared pruning distance
     uint8_t seg[CAP];       // task of the staged particle's cell: its shift is sh[seg]
 };
 
@@ -56,8 +58,8 @@ template <class ST> __device__ __forceinline__ float4 staged_shift(const ST &S, 
     const float *s = S.sh[S.seg[k]];
     return make_float4(s[0], s[1], s[2], S.rad[k]);
 }
-template <bool kDPD, bool kFlux> struct TileOf {
-    using S = StagedT<(kDPD || kFlux) ? kCapX : kCapT, kDPD || kFlux>;
+template <bool kDPD, bool kFlux, bool kSig> struct TileOf {
+    using S = StagedT<(kDPD || kFlux) ? kCapX : kCapT, kDPD || kFlux, kSig>;
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -80,12 +82,13 @@ struct TileArgs {
     int grab;              // work items a warp takes from the shared counter at a time
     int stage_floats;      // table floats and descriptors staged per CTA (TilePlan)
     int stage_pots;
+    int prune;             // stage only neighbour particles within the cutoff of the home cell's bounding box
 };
 
 // Evaluate one interacting pair, reference orientation I = part_i (home), K = part_j.
 // Returns the I-side and K-side increments (force xyz, density) in fI / fK.
 template <bool kDPD, bool kFlux, bool kDensity, class ST>
-__device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P, ST &S, const PotDev *pots,
+__device__ __forceinline__ bool eval_pair(const TileArgs &T, const SimParams &P, ST &S, const PotDev *pots,
                                           const float *blob, int I, int K, float &epot, float &vir, float4 &fI,
                                           float4 &fK, float &qI, float &qK) {
     const PairKernelArgs &a = T.a;
@@ -94,7 +97,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
     const float3 sh = make_float3(s4.x, s4.y, s4.z);
     float3 dx;
     const float r2 = pair_r2(make_float3(pi.x, pi.y, pi.z), sh, make_float3(pk.x, pk.y, pk.z), dx);
-    if (r2 > P.cutoff2) return;   // a candidate that only the table loop's looser filter passed
+    if (r2 > P.cutoff2) return false;   // a candidate that only the table loop's looser filter passed
     const float r = __fsqrt_rn(r2);
     const bool flux_only = kFlux && a.flux_sub >= 0;
     if (kDensity && !flux_only) {
@@ -139,7 +142,7 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
             }
         }
     }
-    if (flux_only) return;
+    if (flux_only) return true;
     const PotDev pot = pots[pidx];
     if (pot.kind == POT_TABLE) {
         float e, f;
@@ -174,112 +177,47 @@ __device__ __forceinline__ void eval_pair(const TileArgs &T, const SimParams &P,
             vir += ftot * ro;
         }
     }
+    return true;
 }
 
-// Evaluate the queued hits held by the active lanes.  Entries are in enumeration order, so
-// equal I mostly form contiguous runs: the I side is summed by a segmented warp scan, and
-// run ends that share an I are combined with match_any.  Equal K are grouped with
-// match_any and summed into the group's lowest lane.  Every accumulator write is then
-// unique within the batch, so plain shared-memory read-modify-writes suffice.
+// Evaluate the queued hits held by the active lanes, one pair per lane.  Both partners'
+// increments (force, number density, and the flux increment of a single staged species) are
+// added straight to the particle arrays with global atomics: a batch holds up to 32 pairs
+// whose partners repeat in no fixed pattern, and the L2 atomics cost less than grouping
+// equal partners within the warp (a segmented scan and match_any) and flushing shared sums.
+// The signature variant counts partners and hashes their ids in the staged sums instead.
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig, class ST>
 __device__ __forceinline__ void eval_batch(const TileArgs &T, const SimParams &P, ST &S, const PotDev *pots,
-                                           const float *blob, bool active, uint32_t e, int lane, float &epot,
-                                           float &vir) {
+                                           const float *blob, bool active, uint32_t e, float &epot, float &vir) {
+    if (!active) return;
     const int I = e & 0xffff, K = e >> 16;
-    if (kSig) {
-        if (active) {
-            // the pair decision proper (the table loop queues candidates with a looser filter)
-            const float4 pi = S.pos[I], pk = S.pos[K], s4 = staged_shift(S, K);
-            float3 dx;
-            if (pair_r2(make_float3(pi.x, pi.y, pi.z), make_float3(s4.x, s4.y, s4.z), make_float3(pk.x, pk.y, pk.z),
-                        dx) > P.cutoff2)
-                return;
-            atomicAdd(reinterpret_cast<int *>(&S.acc[I].x), 1);
-            atomicAdd(reinterpret_cast<int *>(&S.acc[K].x), 1);
-            const uint32_t idi = (uint32_t)__float_as_int(T.a.aux[S.gslot[I]].w);
-            const uint32_t idk = (uint32_t)__float_as_int(T.a.aux[S.gslot[K]].w);
-            atomicAdd(reinterpret_cast<unsigned *>(&S.acc[I].y), sig_mix(idk));
-            atomicAdd(reinterpret_cast<unsigned *>(&S.acc[K].y), sig_mix(idi));
-            record_pair(T.a, (int)idi, (int)idk);
+    if constexpr (kSig) {
+        // the pair decision proper (the table loop queues candidates with a looser filter)
+        const float4 pi = S.pos[I], pk = S.pos[K], s4 = staged_shift(S, K);
+        float3 dx;
+        if (pair_r2(make_float3(pi.x, pi.y, pi.z), make_float3(s4.x, s4.y, s4.z), make_float3(pk.x, pk.y, pk.z), dx) >
+            P.cutoff2)
+            return;
+        atomicAdd(reinterpret_cast<int *>(&S.acc[I].x), 1);
+        atomicAdd(reinterpret_cast<int *>(&S.acc[K].x), 1);
+        const uint32_t idi = (uint32_t)__float_as_int(T.a.aux[S.gslot[I]].w);
+        const uint32_t idk = (uint32_t)__float_as_int(T.a.aux[S.gslot[K]].w);
+        atomicAdd(reinterpret_cast<unsigned *>(&S.acc[I].y), sig_mix(idk));
+        atomicAdd(reinterpret_cast<unsigned *>(&S.acc[K].y), sig_mix(idi));
+        record_pair(T.a, (int)idi, (int)idk);
+    } else {
+        float4 fI = make_float4(0.f, 0.f, 0.f, 0.f), fK = make_float4(0.f, 0.f, 0.f, 0.f);
+        float qI = 0.f, qK = 0.f;   // species 0 flux increments (flux variants, one species)
+        if (!eval_pair<kDPD, kFlux, kDensity>(T, P, S, pots, blob, I, K, epot, vir, fI, fK, qI, qK)) return;
+        const int gI = S.gslot[I], gK = S.gslot[K];
+        if (!(kFlux && T.a.flux_sub >= 0)) {   // a flux-only substep adds no force
+            atomicAdd(&T.a.force[gI], fI);
+            atomicAdd(&T.a.force[gK], fK);
         }
-        return;
-    }
-    float4 fI = make_float4(0.f, 0.f, 0.f, 0.f), fK = make_float4(0.f, 0.f, 0.f, 0.f);
-    float qI = 0.f, qK = 0.f;   // species 0 flux increments (flux variants)
-    if (active) eval_pair<kDPD, kFlux, kDensity>(T, P, S, pots, blob, I, K, epot, vir, fI, fK, qI, qK);
-    // I side: segmented inclusive scan over runs of contiguous lanes with equal I (a run
-    // starts where I differs from the previous lane's)
-    const int key = active ? I : 4096 + lane;
-    const int kprev = __shfl_up_sync(0xffffffffu, key, 1);
-    bool seg = lane == 0 || kprev != key;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const bool s2 = __shfl_up_sync(0xffffffffu, seg, o);
-        const float x = __shfl_up_sync(0xffffffffu, fI.x, o);
-        const float y = __shfl_up_sync(0xffffffffu, fI.y, o);
-        const float z = __shfl_up_sync(0xffffffffu, fI.z, o);
-        const float w = __shfl_up_sync(0xffffffffu, fI.w, o);
-        const float q = kFlux ? __shfl_up_sync(0xffffffffu, qI, o) : 0.f;
-        if (lane >= o && !seg) {
-            fI.x += x; fI.y += y; fI.z += z; fI.w += w;
-            if (kFlux) qI += q;
-            seg = s2;
+        if (kFlux && T.a.nspec == 1) {
+            if (qI != 0.f) atomicAdd(&T.a.sq[gI], qI);
+            if (qK != 0.f) atomicAdd(&T.a.sq[gK], qK);
         }
-    }
-    const int knext = __shfl_down_sync(0xffffffffu, key, 1);
-    // Runs of the same I can recur within a batch (the candidate loop restarts i at each
-    // block of targets): run ends with equal I are combined into the lowest one.
-    const bool run_end = active && (lane == 31 || knext != key);
-    const uint32_t gI = __match_any_sync(0xffffffffu, run_end ? I : 12288 + lane);
-    const uint32_t oI = gI & ~(1u << lane);
-    const int rI = __reduce_max_sync(0xffffffffu, (uint32_t)__popc(oI));
-    const bool leadI = (gI & lanemask_lt()) == 0;
-    uint32_t restI = oI;
-    for (int r = 0; r < rI; r++) {
-        const int src = restI ? __ffs(restI) - 1 : lane;
-        restI &= restI - 1;
-        const float x = __shfl_sync(0xffffffffu, fI.x, src);
-        const float y = __shfl_sync(0xffffffffu, fI.y, src);
-        const float z = __shfl_sync(0xffffffffu, fI.z, src);
-        const float w = __shfl_sync(0xffffffffu, fI.w, src);
-        const float q = kFlux ? __shfl_sync(0xffffffffu, qI, src) : 0.f;
-        if (leadI && src != lane) {
-            fI.x += x; fI.y += y; fI.z += z; fI.w += w;
-            if (kFlux) qI += q;
-        }
-    }
-    // K side: groups of equal K, summed into the lowest lane of each group
-    const int kkey = active ? K : 8192 + lane;
-    const uint32_t grp = __match_any_sync(0xffffffffu, kkey);
-    const uint32_t others = grp & ~(1u << lane);
-    const int rounds = __reduce_max_sync(0xffffffffu, (uint32_t)__popc(others));
-    const bool leader = (grp & lanemask_lt()) == 0;
-    uint32_t rest = others;
-    for (int r = 0; r < rounds; r++) {
-        const int src = rest ? __ffs(rest) - 1 : lane;
-        rest &= rest - 1;
-        const float x = __shfl_sync(0xffffffffu, fK.x, src);
-        const float y = __shfl_sync(0xffffffffu, fK.y, src);
-        const float z = __shfl_sync(0xffffffffu, fK.z, src);
-        const float w = __shfl_sync(0xffffffffu, fK.w, src);
-        const float q = kFlux ? __shfl_sync(0xffffffffu, qK, src) : 0.f;
-        if (leader && src != lane) {
-            fK.x += x; fK.y += y; fK.z += z; fK.w += w;
-            if (kFlux) qK += q;
-        }
-    }
-    if (run_end && leadI) {
-        float4 v = S.acc[I];
-        v.x += fI.x; v.y += fI.y; v.z += fI.z; v.w += fI.w;
-        S.acc[I] = v;
-        if (kFlux) S.sq[I] += qI;
-    }
-    __syncwarp();
-    if (active && leader) {
-        float4 v = S.acc[K];
-        v.x += fK.x; v.y += fK.y; v.z += fK.z; v.w += fK.w;
-        S.acc[K] = v;
-        if (kFlux) S.sq[K] += qK;
     }
 }
 
@@ -298,72 +236,78 @@ __device__ __forceinline__ void flush_red(double *red, int rb, float &epot, floa
     vir = 0.f;
 }
 
+// Stage particles [g0, g0 + n) of one cell at staged index base on, and return how many were
+// staged.  When pruning, a neighbour particle is staged only when its position in the home
+// frame (x + the task's shift) lies within sqrt(S.box[0].w) of the box S.box that holds
+// every home particle: any other one is farther than the cutoff from every home particle,
+// so no pair is lost.  Staged particles keep their cell order.
 template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __forceinline__ void stage_body(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task,
-                                           int lane) {
+__device__ __forceinline__ int stage_body(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task,
+                                          int lane, bool prune) {
+    int kept = 0;
+    const float *sh = S.sh[task];
 #pragma unroll 1
-    for (int k = lane; k < n; k += 32) {
-        const int g = g0 + k;
-        const float4 ax = a.aux[g];
-        S.pos[base + k] = a.pos[g];
-        S.acc[base + k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        S.gslot[base + k] = g;
-        S.rad[base + k] = ax.x;
-        S.seg[base + k] = (uint8_t)task;
-        if (!kSig && kDPD) {
-            S.vel[base + k] = a.vel[g];
-            S.id[base + k] = __float_as_int(ax.w);
+    for (int k0 = 0; k0 < n; k0 += 32) {
+        const int k = k0 + lane;
+        bool keep = k < n;
+        const int g = g0 + (keep ? k : 0);
+        const float4 p = a.pos[g];
+        if (prune) {
+            const float4 lo = S.box[0], hi = S.box[1];
+            const float xs = p.x + sh[0], ys = p.y + sh[1], zs = p.z + sh[2];
+            const float dx = fmaxf(fmaxf(lo.x - xs, xs - hi.x), 0.f);
+            const float dy = fmaxf(fmaxf(lo.y - ys, ys - hi.y), 0.f);
+            const float dz = fmaxf(fmaxf(lo.z - zs, zs - hi.z), 0.f);
+            keep = keep && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= lo.w;
         }
-        if (!kSig && kFlux) {
-            S.sv[base + k] = a.sval[g];
-            S.sq[base + k] = 0.f;
+        const uint32_t m = __ballot_sync(0xffffffffu, keep);
+        if (keep) {
+            const int d = base + kept + __popc(m & lanemask_lt());
+            const float4 ax = a.aux[g];
+            S.pos[d] = p;
+            if (kSig) S.acc[d] = make_float4(0.f, 0.f, 0.f, 0.f);
+            S.gslot[d] = g;
+            S.rad[d] = ax.x;
+            S.seg[d] = (uint8_t)task;
+            if (!kSig && kDPD) {
+                S.vel[d] = a.vel[g];
+                S.id[d] = __float_as_int(ax.w);
+            }
+            if (!kSig && kFlux) S.sv[d] = a.sval[g];
         }
+        kept += __popc(m);
     }
+    return kept;
 }
 
-template <bool kFlux, bool kSig, class ST>
-__device__ __forceinline__ void flush_body(const PairKernelArgs &a, ST &S, int b0, int b1, int lane) {
+// Signature variant: add the staged partner counts and id hashes to the per-id totals.
+template <class ST>
+__device__ __forceinline__ void flush_sig(const PairKernelArgs &a, ST &S, int b0, int b1, int lane) {
 #pragma unroll 1
     for (int k = b0 + lane; k < b1; k += 32) {
         const float4 v = S.acc[k];
-        const int g = S.gslot[k];
-        if (kSig) {
-            const int c = __float_as_int(v.x);
-            if (c) {
-                const int id = __float_as_int(a.aux[g].w);
-                atomicAdd(&a.sig_count[id], c);
-                atomicAdd(&a.sig_hash[id], (uint32_t)__float_as_int(v.y));
-            }
-            continue;
-        }
-        if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) atomicAdd(&a.force[g], v);
-        if (kFlux) {
-            const float q = S.sq[k];
-            if (q != 0.f) atomicAdd(&a.sq[g], q);
+        const int c = __float_as_int(v.x);
+        if (c) {
+            const int id = __float_as_int(a.aux[S.gslot[k]].w);
+            atomicAdd(&a.sig_count[id], c);
+            atomicAdd(&a.sig_hash[id], (uint32_t)__float_as_int(v.y));
         }
     }
 }
 
-// Staging and flushing run once per segment, not per pair.  Out of line they keep the hot
-// candidate/evaluation loop of the table variants small in instruction cache; the DPD and
-// flux variants, whose evaluation is inlined once, run faster with them inline.
+// Staging runs once per segment, not per pair.  Out of line it keeps the hot candidate and
+// evaluation loop of the table variants small in instruction cache; the DPD and flux
+// variants, whose evaluation is inlined once, run faster with it inline.
 template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __noinline__ void stage_call(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane) {
-    stage_body<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane);
-}
-template <bool kFlux, bool kSig, class ST>
-__device__ __noinline__ void flush_call(const PairKernelArgs &a, ST &S, int b0, int b1, int lane) {
-    flush_body<kFlux, kSig>(a, S, b0, b1, lane);
+__device__ __noinline__ int stage_call(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane,
+                                       bool prune) {
+    return stage_body<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane, prune);
 }
 template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __forceinline__ void stage(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane) {
-    if constexpr (kDPD || kFlux) stage_body<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane);
-    else stage_call<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane);
-}
-template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __forceinline__ void flush(const PairKernelArgs &a, ST &S, int b0, int b1, int lane) {
-    if constexpr (kDPD || kFlux) flush_body<kFlux, kSig>(a, S, b0, b1, lane);
-    else flush_call<kFlux, kSig>(a, S, b0, b1, lane);
+__device__ __forceinline__ int stage(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane,
+                                     bool prune) {
+    if constexpr (kDPD || kFlux) return stage_body<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane, prune);
+    else return stage_call<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane, prune);
 }
 
 // kVerlet (table variants): simulations in Verlet mode record, on their rebuild steps, the
@@ -372,7 +316,7 @@ __device__ __forceinline__ void flush(const PairKernelArgs &a, ST &S, int b0, in
 // keeps its sorted windows between rebuilds instead, tf_runner_dopair.cpp:115-117).
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false, int kW = kWarps>
 __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
-    using Staged = typename TileOf<kDPD, kFlux>::S;
+    using Staged = typename TileOf<kDPD, kFlux, kSig>::S;
     constexpr int kCap = Staged::cap;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Staged *L = reinterpret_cast<Staged *>(smem_raw);
@@ -462,8 +406,36 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
             if (kVerlet && lmode == 1 && lane == 0) a.vlen[item] = -1;
             continue;
         }
-        stage<kDPD, kFlux, kSig>(a, S, 0, h0, nh, 13, lane);
+        stage<kDPD, kFlux, kSig>(a, S, 0, h0, nh, 13, lane, false);
         __syncwarp();
+        // the box that holds every home particle, for the neighbour staging's pruning, with the
+        // squared cutoff and a 1e-4 relative margin (far above the few-ulp difference between
+        // this box distance and the reference's r2)
+        const bool prune = !kVerlet && T.prune && t1 > 14;
+        if (prune) {
+            float4 blo = make_float4(3.0e38f, 3.0e38f, 3.0e38f, cutoff2 * 1.0001f);
+            float4 bhi = make_float4(-3.0e38f, -3.0e38f, -3.0e38f, 0.f);
+#pragma unroll 1
+            for (int k = lane; k < nh; k += 32) {
+                const float4 p4 = S.pos[k];
+                blo.x = fminf(blo.x, p4.x); blo.y = fminf(blo.y, p4.y); blo.z = fminf(blo.z, p4.z);
+                bhi.x = fmaxf(bhi.x, p4.x); bhi.y = fmaxf(bhi.y, p4.y); bhi.z = fmaxf(bhi.z, p4.z);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                blo.x = fminf(blo.x, __shfl_xor_sync(0xffffffffu, blo.x, o));
+                blo.y = fminf(blo.y, __shfl_xor_sync(0xffffffffu, blo.y, o));
+                blo.z = fminf(blo.z, __shfl_xor_sync(0xffffffffu, blo.z, o));
+                bhi.x = fmaxf(bhi.x, __shfl_xor_sync(0xffffffffu, bhi.x, o));
+                bhi.y = fmaxf(bhi.y, __shfl_xor_sync(0xffffffffu, bhi.y, o));
+                bhi.z = fmaxf(bhi.z, __shfl_xor_sync(0xffffffffu, bhi.z, o));
+            }
+            if (lane == 0) {
+                S.box[0] = blo;
+                S.box[1] = bhi;
+            }
+            __syncwarp();
+        }
         // wall potentials of the home particles, once per home cell (runner_doself's
         // boundary_eval, tf_runner_dopair.cpp:594-596)
         if (!kSig && t0 == 13 && a.has_wall_pots && P.walls_active && !(kFlux && a.flux_sub >= 0)) {
@@ -475,9 +447,7 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
                 float ew = 0.f;
                 wall_eval(P, a.wpots, blob, __float_as_int(p4.w), make_float3(p4.x, p4.y, p4.z), S.rad[k],
                           a.vel[g], __float_as_int(a.aux[g].w) - P.id_off, li, lj, lk, fw, ew);
-                S.acc[k].x += fw.x;
-                S.acc[k].y += fw.y;
-                S.acc[k].z += fw.z;
+                if (fw.x != 0.f || fw.y != 0.f || fw.z != 0.f) atomicAdd(&a.force[g], make_float4(fw.x, fw.y, fw.z, 0.f));
                 epot += ew;
             }
             __syncwarp();
@@ -496,8 +466,7 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
                 const int g0 = __shfl_sync(0xffffffffu, my_g0, t - 14);
                 const int nn = __shfl_sync(0xffffffffu, my_n, t - 14);
                 if (end + nn > kCap) break;
-                if (nn > 0) stage<kDPD, kFlux, kSig>(a, S, end, g0, nn, t, lane);
-                end += nn;
+                if (nn > 0) end += stage<kDPD, kFlux, kSig>(a, S, end, g0, nn, t, lane, prune);
                 t++;
             }
             __syncwarp();
@@ -549,7 +518,7 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
                         const int take = avail < 32 ? avail : 32;
                         const bool act = lane < take;
                         const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
-                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, lane, epot, vir);
+                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, epot, vir);
                         qhead += take;
                         __syncwarp();
                     } else if (done) {
@@ -597,7 +566,7 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
                         const int take = avail < 32 ? avail : 32;
                         const bool act = lane < take;
                         const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
-                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, lane, epot, vir);
+                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, epot, vir);
                         qhead += take;
                         __syncwarp();
                     }
@@ -640,7 +609,7 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
                             __syncwarp();
                             if (qtail - qhead >= 32) {
                                 const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
-                                eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, true, e, lane, epot, vir);
+                                eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, true, e, epot, vir);
                                 qhead += 32;
                                 __syncwarp();
                             }
@@ -649,7 +618,7 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
                     if (qtail > qhead) {
                         const bool act = lane < qtail - qhead;
                         const uint32_t e = act ? S.q[(qhead + lane) & (kQ - 1)] : 0u;
-                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, lane, epot, vir);
+                        eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, act, e, epot, vir);
                     }
                 }
                 __syncwarp();
@@ -658,10 +627,10 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
                 if (lane == 0 && lcount < a.list_k) lst[list_slot(lcount)] = kListEnd;
                 lcount = (lcount + 128) & ~127;
             }
-            flush<kDPD, kFlux, kSig>(a, S, nh, end, lane);
+            if (kSig) flush_sig(a, S, nh, end, lane);
             __syncwarp();
         }
-        flush<kDPD, kFlux, kSig>(a, S, 0, nh, lane);
+        if (kSig) flush_sig(a, S, 0, nh, lane);
         if (kVerlet && lmode == 1 && lane == 0) {
             a.vlen[item] = lcount <= a.list_k ? lcount : -1;
             atomicMax(a.list_need, lcount);
@@ -812,7 +781,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
 
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig, bool kVerlet = false, int kW = kWarps>
 void launch_variant(const TileArgs &T0, cudaStream_t s, int sms) {
-    const size_t base = sizeof(typename TileOf<kDPD, kFlux>::S) * kW;
+    const size_t base = sizeof(typename TileOf<kDPD, kFlux, kSig>::S) * kW;
     const size_t smem_max = base + sizeof(float) * kMaxSmemTable + sizeof(PotDev) * kMaxSmemPots;
     // Tables and descriptors are staged only while a CTA still fits 32 / kW per SM (four of 8
     // warps): those CTAs are worth more than shared-memory tables (the table variants' staging
@@ -858,6 +827,7 @@ void launch_pair_overflow(const PairKernelArgs &a, int *overflow_list, int *over
     T.grab = 1;
     T.stage_floats = 0;
     T.stage_pots = 0;
+    T.prune = 0;
     if (signature) k_pair_overflow<false, false, false, true><<<sms, 256, 0, s>>>(T);
     else if (!(a.flags & TFG_ENGINE_NO_DENSITY)) k_pair_overflow<false, false, true, false><<<sms, 256, 0, s>>>(T);
     else k_pair_overflow<false, false, false, false><<<sms, 256, 0, s>>>(T);
@@ -877,6 +847,7 @@ void launch_pair_fluxonly(const PairKernelArgs &a, const TilePlan &plan, int *ov
     T.grab = 1;
     T.stage_floats = plan.stage_floats;
     T.stage_pots = plan.stage_pots;
+    T.prune = 1;
     cudaMemsetAsync(overflow_count, 0, 2 * sizeof(int), s);
     if (a.n <= 0) return;
     launch_variant<false, true, false, false>(T, s, sms);
@@ -902,6 +873,7 @@ void launch_pair_tile(const PairKernelArgs &a, const TilePlan &plan, int *overfl
     T.grab = tune.grab >= 1 && tune.grab <= 8 ? tune.grab : 1;
     T.stage_floats = plan.stage_floats;
     T.stage_pots = plan.stage_pots;
+    T.prune = 1;
     cudaMemsetAsync(overflow_count, 0, 2 * sizeof(int), s);
     if (a.n <= 0) return;
     const bool dpd = a.has_dpd, flux = a.nspec > 0 && a.has_flux;
