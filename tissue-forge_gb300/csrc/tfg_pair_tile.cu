@@ -29,7 +29,10 @@ constexpr int kWarps = 8;
 constexpr int kCapT = 156;          // staged particles per warp (table variants)
 constexpr int kCapX = 88;           // staged particles per warp (DPD and flux variants)
 constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
-constexpr int kQ = 64;              // candidate ring queue entries per warp (power of two)
+constexpr int kUnroll = 2;          // home particles tested per pass of the table variants' candidate loop
+static_assert(kHomeCap + kUnroll <= kCapT, "the unrolled candidate loop reads up to kUnroll - 1 past the home cell");
+constexpr int kQ = 128;             // candidate ring queue entries per warp (power of two, >= 31 + 32 kUnroll)
+static_assert(kQ >= 31 + 32 * kUnroll, "a pass queues up to 32 kUnroll hits onto at most 31 waiting ones");
 constexpr int kMaxSmemTable = 4096; // floats of potential table staged per CTA
 constexpr int kMaxSmemPots = 64;    // potential descriptors staged per CTA (all simulations)
 constexpr size_t kFourCtaBytes = 228 * 1024 / 4 - 1024;   // dynamic shared memory of a CTA, four per SM
@@ -588,30 +591,60 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
                         const int iend = kb + 31 < nh ? kb + 31 : nh;
                         const float xs = pk.x + s4.x, ys = pk.y + s4.y, zs = pk.z + s4.z;
                         const float cut_f = cutoff2 * 1.00001f;
-                        for (int i = 0; i < iend; i++) {
-                            const float4 pi4 = S.pos[i];
-                            const float ddx = pi4.x - xs, ddy = pi4.y - ys, ddz = pi4.z - zs;
-                            const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
-                            const bool hit = i < ilim && r2 <= cut_f;
-                            if (kVerlet && lmode == 1) {
-                                const bool lh = i < ilim && r2 <= rlist2;
-                                const uint32_t lm = __ballot_sync(0xffffffffu, lh);
-                                if (lh) {
-                                    const int lp = lcount + __popc(lm & lanemask_lt());
-                                    if (lp < a.list_k) lst[list_slot(lp)] = (uint32_t)i | ((uint32_t)k << 16);
+                        if constexpr (kVerlet) {
+                            for (int i = 0; i < iend; i++) {
+                                const float4 pi4 = S.pos[i];
+                                const float ddx = pi4.x - xs, ddy = pi4.y - ys, ddz = pi4.z - zs;
+                                const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
+                                const bool hit = i < ilim && r2 <= cut_f;
+                                if (lmode == 1) {
+                                    const bool lh = i < ilim && r2 <= rlist2;
+                                    const uint32_t lm = __ballot_sync(0xffffffffu, lh);
+                                    if (lh) {
+                                        const int lp = lcount + __popc(lm & lanemask_lt());
+                                        if (lp < a.list_k) lst[list_slot(lp)] = (uint32_t)i | ((uint32_t)k << 16);
+                                    }
+                                    lcount += __popc(lm);
                                 }
-                                lcount += __popc(lm);
-                            }
-                            const uint32_t m = __ballot_sync(0xffffffffu, hit);
-                            if (hit)
-                                S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)k << 16);
-                            qtail += __popc(m);
-                            __syncwarp();
-                            if (qtail - qhead >= 32) {
-                                const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
-                                eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, true, e, epot, vir);
-                                qhead += 32;
+                                const uint32_t m = __ballot_sync(0xffffffffu, hit);
+                                if (hit)
+                                    S.q[(qtail + __popc(m & lanemask_lt())) & (kQ - 1)] = (uint32_t)i | ((uint32_t)k << 16);
+                                qtail += __popc(m);
                                 __syncwarp();
+                                if (qtail - qhead >= 32) {
+                                    const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
+                                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, true, e, epot, vir);
+                                    qhead += 32;
+                                    __syncwarp();
+                                }
+                            }
+                        } else {
+                            // kUnroll home particles per pass share the queue bookkeeping; i < ilim
+                            // implies i < iend, so the reads past iend (still inside pos[]) are
+                            // never queued
+                            const uint32_t lt = lanemask_lt();
+                            for (int i = 0; i < iend; i += kUnroll) {
+                                int add = 0;
+#pragma unroll
+                                for (int u = 0; u < kUnroll; u++) {
+                                    const int ii = i + u;
+                                    const float4 pi4 = S.pos[ii];
+                                    const float ddx = pi4.x - xs, ddy = pi4.y - ys, ddz = pi4.z - zs;
+                                    const float r2 = fmaf(ddx, ddx, fmaf(ddy, ddy, ddz * ddz));
+                                    const bool hit = ii < ilim && r2 <= cut_f;
+                                    const uint32_t m = __ballot_sync(0xffffffffu, hit);
+                                    if (hit)
+                                        S.q[(qtail + add + __popc(m & lt)) & (kQ - 1)] = (uint32_t)ii | ((uint32_t)k << 16);
+                                    add += __popc(m);
+                                }
+                                qtail += add;
+                                __syncwarp();
+                                while (qtail - qhead >= 32) {
+                                    const uint32_t e = S.q[(qhead + lane) & (kQ - 1)];
+                                    eval_batch<kDPD, kFlux, kDensity, kSig>(T, P, S, spots, blob, true, e, epot, vir);
+                                    qhead += 32;
+                                    __syncwarp();
+                                }
                             }
                         }
                     }
