@@ -53,6 +53,8 @@ template <int CAP, bool EXTRA, bool SIG> struct StagedT {
     int32_t id[EXTRA ? CAP : 1];
     float sv[EXTRA ? CAP : 1];   // species 0 value
     float4 box[2];          // box holding every home particle (lo, hi); lo.w: squared pruning distance
+    int32_t toff[13];       // flat staging: offset of forward task 14 + L's particles in the flat list
+    int32_t tg0[13];        // flat staging: first slot of forward task 14 + L's cell
     uint8_t seg[CAP];       // task of the staged particle's cell: its shift is sh[seg]
 };
 
@@ -298,6 +300,64 @@ __device__ __forceinline__ void flush_sig(const PairKernelArgs &a, ST &S, int b0
     }
 }
 
+// Stage, after the home cell, every particle of the forward tasks whose offsets and first
+// slots are in S.toff / S.tg0 (total particles in all), in one pass over the flat list, so
+// that the loads of all cells are in flight together rather than one cell after another.
+// Pruning and order are those of stage_body.  Returns the number staged.
+template <bool kDPD, bool kFlux, bool kSig, class ST>
+__device__ __forceinline__ int stage_flat_body(const PairKernelArgs &a, ST &S, int base, int total, int lane,
+                                               bool prune) {
+    int kept = 0;
+#pragma unroll 1
+    for (int b0 = 0; b0 < total; b0 += 64) {
+        // two lanes' worth of particles per pass: both loads issue before either is used
+        int g[2], tk[2];
+        float4 p[2], ax[2];
+        bool keep[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int idx = b0 + 32 * h + lane;
+            keep[h] = idx < total;
+            int L = 0;   // the last forward task whose flat offset is <= idx
+#pragma unroll
+            for (int st = 8; st > 0; st >>= 1)
+                if (L + st < 13 && S.toff[L + st] <= idx) L += st;
+            tk[h] = 14 + L;
+            g[h] = keep[h] ? S.tg0[L] + (idx - S.toff[L]) : 0;   // slot 0 exists: the pass has particles
+            p[h] = a.pos[g[h]];
+            ax[h] = a.aux[g[h]];
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            if (prune && keep[h]) {
+                const float4 lo = S.box[0], hi = S.box[1];
+                const float *sh = S.sh[tk[h]];
+                const float xs = p[h].x + sh[0], ys = p[h].y + sh[1], zs = p[h].z + sh[2];
+                const float dx = fmaxf(fmaxf(lo.x - xs, xs - hi.x), 0.f);
+                const float dy = fmaxf(fmaxf(lo.y - ys, ys - hi.y), 0.f);
+                const float dz = fmaxf(fmaxf(lo.z - zs, zs - hi.z), 0.f);
+                keep[h] = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= lo.w;
+            }
+            const uint32_t m = __ballot_sync(0xffffffffu, keep[h]);
+            if (keep[h]) {
+                const int d = base + kept + __popc(m & lanemask_lt());
+                S.pos[d] = p[h];
+                if (kSig) S.acc[d] = make_float4(0.f, 0.f, 0.f, 0.f);
+                S.gslot[d] = g[h];
+                S.rad[d] = ax[h].x;
+                S.seg[d] = (uint8_t)tk[h];
+                if (!kSig && kDPD) {
+                    S.vel[d] = a.vel[g[h]];
+                    S.id[d] = __float_as_int(ax[h].w);
+                }
+                if (!kSig && kFlux) S.sv[d] = a.sval[g[h]];
+            }
+            kept += __popc(m);
+        }
+    }
+    return kept;
+}
+
 // Staging runs once per segment, not per pair.  Out of line it keeps the hot candidate and
 // evaluation loop of the table variants small in instruction cache; the DPD and flux
 // variants, whose evaluation is inlined once, run faster with it inline.
@@ -305,6 +365,15 @@ template <bool kDPD, bool kFlux, bool kSig, class ST>
 __device__ __noinline__ int stage_call(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane,
                                        bool prune) {
     return stage_body<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane, prune);
+}
+template <bool kDPD, bool kFlux, bool kSig, class ST>
+__device__ __noinline__ int stage_flat_call(const PairKernelArgs &a, ST &S, int base, int total, int lane, bool prune) {
+    return stage_flat_body<kDPD, kFlux, kSig>(a, S, base, total, lane, prune);
+}
+template <bool kDPD, bool kFlux, bool kSig, class ST>
+__device__ __forceinline__ int stage_flat(const PairKernelArgs &a, ST &S, int base, int total, int lane, bool prune) {
+    if constexpr (kDPD || kFlux) return stage_flat_body<kDPD, kFlux, kSig>(a, S, base, total, lane, prune);
+    else return stage_flat_call<kDPD, kFlux, kSig>(a, S, base, total, lane, prune);
 }
 template <bool kDPD, bool kFlux, bool kSig, class ST>
 __device__ __forceinline__ int stage(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane,
@@ -353,6 +422,10 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
     if (lane == 0) base = atomicAdd(T.overflow_count + 1, grab);
     base = __shfl_sync(0xffffffffu, base, 0);
     for (; base < nitems;) {
+    // the next items are reserved now and read after these, so the atomic's round trip
+    // overlaps this work instead of adding to it
+    int nxt = 0;
+    if (lane == 0) nxt = atomicAdd(T.overflow_count + 1, grab);
 #pragma unroll 1
     for (int item = base; item < base + grab && item < nitems; item++) {
         const int home = item / T.split, grp = item - home * T.split;
@@ -458,13 +531,40 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
 
         int t = t0 < 14 ? 14 : t0;     // next neighbour task to stage
         bool with_self = (t0 == 13);
-        while (with_self || t < t1) {
+        // When the home cell and every neighbour of this work item fit at once (the usual
+        // case), they are staged in one flat pass, in the same order as segment by segment.
+        int flat_n = -1;
+        if (t < t1) {
+            const bool inc = lane >= t - 14 && lane < t1 - 14;
+            const int cnt = inc ? my_n : 0;
+            int incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 16; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, incl, 15);
+            if (nh + total <= kCap) {
+                if (lane < 13) {
+                    S.toff[lane] = lane < t - 14 ? -1 : (inc ? incl - cnt : 0x7fffffff);
+                    S.tg0[lane] = my_g0;
+                }
+                __syncwarp();
+                flat_n = total > 0 ? stage_flat<kDPD, kFlux, kSig>(a, S, nh, total, lane, prune) : 0;
+                t = t1;
+            }
+        }
+        while (with_self || t < t1 || flat_n >= 0) {
             // walk: the chunk's first group of list entries loads while its segments are staged
             uint4 gnext = make_uint4(kListEnd, kListEnd, kListEnd, kListEnd);
             if (kVerlet && lmode == 2 && lcount + 4 * lane < lvalid)
                 gnext = *reinterpret_cast<const uint4 *>(lst + lcount + 4 * lane);
             // stage as many neighbour segments as fit after the home cell
             int end = nh;
+            if (flat_n >= 0) {
+                end = nh + flat_n;
+                flat_n = -1;
+            }
             while (t < t1) {
                 const int g0 = __shfl_sync(0xffffffffu, my_g0, t - 14);
                 const int nn = __shfl_sync(0xffffffffu, my_n, t - 14);
@@ -670,8 +770,7 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
         }
         __syncwarp();
     }
-    if (lane == 0) base = atomicAdd(T.overflow_count + 1, grab);
-    base = __shfl_sync(0xffffffffu, base, 0);
+    base = __shfl_sync(0xffffffffu, nxt, 0);
     }
     if (kSig) return;
     flush_red(a.red, cur_rb, epot, vir, lane);
