@@ -26,8 +26,8 @@ namespace tfg {
 namespace {
 
 constexpr int kWarps = 8;
-constexpr int kCapT = 156;          // staged particles per warp (table variants)
-constexpr int kCapX = 88;           // staged particles per warp (DPD and flux variants)
+constexpr int kCapT = 200;          // staged particles per warp (table variants)
+constexpr int kCapX = 120;          // staged particles per warp (DPD and flux variants)
 constexpr int kHomeCap = 96;        // largest home cell handled by the tiled kernel
 constexpr int kUnroll = 2;          // home particles tested per pass of the table variants' candidate loop
 static_assert(kHomeCap + kUnroll <= kCapT, "the unrolled candidate loop reads up to kUnroll - 1 past the home cell");
@@ -66,6 +66,8 @@ template <class ST> __device__ __forceinline__ float4 staged_shift(const ST &S, 
 template <bool kDPD, bool kFlux, bool kSig> struct TileOf {
     using S = StagedT<(kDPD || kFlux) ? kCapX : kCapT, kDPD || kFlux, kSig>;
 };
+static_assert(sizeof(TileOf<false, false, false>::S) * kWarps <= kFourCtaBytes, "table variants: four CTAs per SM");
+static_assert(sizeof(TileOf<true, true, false>::S) * kWarps <= kFourCtaBytes, "DPD and flux variants: four CTAs per SM");
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
@@ -300,16 +302,16 @@ __device__ __forceinline__ void flush_sig(const PairKernelArgs &a, ST &S, int b0
     }
 }
 
-// Stage, after the home cell, every particle of the forward tasks whose offsets and first
-// slots are in S.toff / S.tg0 (total particles in all), in one pass over the flat list, so
-// that the loads of all cells are in flight together rather than one cell after another.
-// Pruning and order are those of stage_body.  Returns the number staged.
+// Stage entries [f0, f1) of the flat list of this work item's neighbour particles (the
+// forward tasks' offsets and first slots are in S.toff / S.tg0) at staged index base on, in
+// passes of 64 whose loads are in flight together.  Pruning and order are those of
+// stage_body.  Returns the number staged.
 template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __forceinline__ int stage_flat_body(const PairKernelArgs &a, ST &S, int base, int total, int lane,
+__device__ __forceinline__ int stage_flat_body(const PairKernelArgs &a, ST &S, int base, int f0, int f1, int lane,
                                                bool prune) {
     int kept = 0;
 #pragma unroll 1
-    for (int b0 = 0; b0 < total; b0 += 64) {
+    for (int b0 = f0; b0 < f1; b0 += 64) {
         // two lanes' worth of particles per pass: both loads issue before either is used
         int g[2], tk[2];
         float4 p[2], ax[2];
@@ -317,7 +319,7 @@ __device__ __forceinline__ int stage_flat_body(const PairKernelArgs &a, ST &S, i
 #pragma unroll
         for (int h = 0; h < 2; h++) {
             const int idx = b0 + 32 * h + lane;
-            keep[h] = idx < total;
+            keep[h] = idx < f1;
             int L = 0;   // the last forward task whose flat offset is <= idx
 #pragma unroll
             for (int st = 8; st > 0; st >>= 1)
@@ -367,13 +369,15 @@ __device__ __noinline__ int stage_call(const PairKernelArgs &a, ST &S, int base,
     return stage_body<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane, prune);
 }
 template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __noinline__ int stage_flat_call(const PairKernelArgs &a, ST &S, int base, int total, int lane, bool prune) {
-    return stage_flat_body<kDPD, kFlux, kSig>(a, S, base, total, lane, prune);
+__device__ __noinline__ int stage_flat_call(const PairKernelArgs &a, ST &S, int base, int f0, int f1, int lane,
+                                            bool prune) {
+    return stage_flat_body<kDPD, kFlux, kSig>(a, S, base, f0, f1, lane, prune);
 }
 template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __forceinline__ int stage_flat(const PairKernelArgs &a, ST &S, int base, int total, int lane, bool prune) {
-    if constexpr (kDPD || kFlux) return stage_flat_body<kDPD, kFlux, kSig>(a, S, base, total, lane, prune);
-    else return stage_flat_call<kDPD, kFlux, kSig>(a, S, base, total, lane, prune);
+__device__ __forceinline__ int stage_flat(const PairKernelArgs &a, ST &S, int base, int f0, int f1, int lane,
+                                          bool prune) {
+    if constexpr (kDPD || kFlux) return stage_flat_body<kDPD, kFlux, kSig>(a, S, base, f0, f1, lane, prune);
+    else return stage_flat_call<kDPD, kFlux, kSig>(a, S, base, f0, f1, lane, prune);
 }
 template <bool kDPD, bool kFlux, bool kSig, class ST>
 __device__ __forceinline__ int stage(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane,
@@ -472,9 +476,9 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
         }
         if (lane == 13) { S.sh[13][0] = 0.f; S.sh[13][1] = 0.f; S.sh[13][2] = 0.f; }
         __syncwarp();
-        // capacity: every group of this home cell takes the same decision
-        const bool over = nh > kHomeCap || (lane < 13 && nh + my_n > kCap);
-        if (__any_sync(0xffffffffu, over)) {
+        // capacity: a home cell above kHomeCap goes to the overflow pass (every group of the
+        // cell takes the same decision); neighbour cells of any size are staged in chunks
+        if (nh > kHomeCap) {
             if (lane == 0 && grp == 0) {
                 const int k = atomicAdd(T.overflow_count, 1);
                 T.overflow_list[k] = home;
@@ -529,13 +533,13 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
             __syncwarp();
         }
 
-        int t = t0 < 14 ? 14 : t0;     // next neighbour task to stage
+        // The neighbour cells of this work item form one flat list (task order, cell order);
+        // each chunk stages as much of it as fits after the home cell.
+        const int tf = t0 < 14 ? 14 : t0;     // first neighbour task of this item
         bool with_self = (t0 == 13);
-        // When the home cell and every neighbour of this work item fit at once (the usual
-        // case), they are staged in one flat pass, in the same order as segment by segment.
-        int flat_n = -1;
-        if (t < t1) {
-            const bool inc = lane >= t - 14 && lane < t1 - 14;
+        int total = 0;
+        if (tf < t1) {
+            const bool inc = lane >= tf - 14 && lane < t1 - 14;
             const int cnt = inc ? my_n : 0;
             int incl = cnt;
 #pragma unroll
@@ -543,34 +547,24 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
                 const int v = __shfl_up_sync(0xffffffffu, incl, o);
                 if (lane >= o) incl += v;
             }
-            const int total = __shfl_sync(0xffffffffu, incl, 15);
-            if (nh + total <= kCap) {
-                if (lane < 13) {
-                    S.toff[lane] = lane < t - 14 ? -1 : (inc ? incl - cnt : 0x7fffffff);
-                    S.tg0[lane] = my_g0;
-                }
-                __syncwarp();
-                flat_n = total > 0 ? stage_flat<kDPD, kFlux, kSig>(a, S, nh, total, lane, prune) : 0;
-                t = t1;
+            total = __shfl_sync(0xffffffffu, incl, 15);
+            if (lane < 13) {
+                S.toff[lane] = lane < tf - 14 ? -1 : (inc ? incl - cnt : 0x7fffffff);
+                S.tg0[lane] = my_g0;
             }
+            __syncwarp();
         }
-        while (with_self || t < t1 || flat_n >= 0) {
-            // walk: the chunk's first group of list entries loads while its segments are staged
+        int fpos = 0;   // next flat entry to stage
+        while (with_self || fpos < total) {
+            // walk: the chunk's first group of list entries loads while its particles are staged
             uint4 gnext = make_uint4(kListEnd, kListEnd, kListEnd, kListEnd);
             if (kVerlet && lmode == 2 && lcount + 4 * lane < lvalid)
                 gnext = *reinterpret_cast<const uint4 *>(lst + lcount + 4 * lane);
-            // stage as many neighbour segments as fit after the home cell
             int end = nh;
-            if (flat_n >= 0) {
-                end = nh + flat_n;
-                flat_n = -1;
-            }
-            while (t < t1) {
-                const int g0 = __shfl_sync(0xffffffffu, my_g0, t - 14);
-                const int nn = __shfl_sync(0xffffffffu, my_n, t - 14);
-                if (end + nn > kCap) break;
-                if (nn > 0) end += stage<kDPD, kFlux, kSig>(a, S, end, g0, nn, t, lane, prune);
-                t++;
+            if (fpos < total) {   // nh <= kHomeCap < kCap, so every chunk takes at least one entry
+                const int take = min(total - fpos, kCap - end);
+                end += stage_flat<kDPD, kFlux, kSig>(a, S, end, fpos, fpos + take, lane, prune);
+                fpos += take;
             }
             __syncwarp();
             const int tbeg = with_self ? 0 : nh;
