@@ -103,12 +103,14 @@ def test_least_work_first_among_arrived_requests(fake):
             for i, (n, steps) in enumerate([(800, 20), (900, 30), (300, 5), (600, 4), (700, 40)])]
     srv = Server(max_particles=1000, quantum=64, lib=fake)
     done = srv.run(reqs)
-    order = [r.rid for r in sorted(done, key=lambda r: (r.t_admit, r.rid))]
+    # the server's own admission times order the admissions exactly (requests admitted in the
+    # same turn are mapped onto the client clock through their own submission times)
+    order = [r.rid for r in sorted(done, key=lambda r: r.t_admit_server)]
     assert order == sorted(range(5), key=lambda i: reqs[i].workload.n * reqs[i].steps)
     reqs2 = [Request(r.rid, 0.0, r.workload, r.steps) for r in reqs]
     srv = Server(max_particles=1000, quantum=64, policy="fifo", lib=fake)
     done = srv.run(reqs2)
-    assert [r.rid for r in sorted(done, key=lambda r: (r.t_admit, r.rid))] == list(range(5))
+    assert [r.rid for r in sorted(done, key=lambda r: r.t_admit_server)] == list(range(5))
     for r in done:
         assert np.all(r.result["x"] == r.steps)
 

@@ -770,17 +770,24 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
     flush_red(a.red, cur_rb, epot, vir, lane);
 }
 
-// Home cells whose own or neighbour population exceeds the staging capacity: one warp
-// per listed home cell, candidates read from global memory, accumulation with global
-// atomics.  Same orientation and arithmetic as the tiled kernel.
+// Home cells above the tiled kernel's home capacity (crowded clusters): candidates read
+// from global memory, accumulation with global atomics, same orientation and arithmetic as
+// the tiled kernel.  The work of one listed cell is spread over 14 x kOverflowParts warps
+// (task, and a share of the task's candidate pairs), so that one crowded cell does not
+// leave a single warp working while the rest of the GPU waits.
+constexpr int kOverflowParts = 8;
 template <bool kDPD, bool kFlux, bool kDensity, bool kSig>
 __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
     const PairKernelArgs &a = T.a;
     const int lane = threadIdx.x & 31;
     const int nlist = *T.overflow_count;
     float epot = 0.f, vir = 0.f;
-    for (int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nlist; w += (gridDim.x * blockDim.x) >> 5) {
-        const int home = T.overflow_list[w];
+    const long long nwork = (long long)nlist * 14 * kOverflowParts;
+    for (long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; w < nwork;
+         w += ((long long)gridDim.x * blockDim.x) >> 5) {
+        const int home = T.overflow_list[w / (14 * kOverflowParts)];
+        const int d = 13 + (int)((w / kOverflowParts) % 14);   // this warp's task
+        const int part = (int)(w % kOverflowParts);             // and its share of the pairs
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         const SimParams &P = a.sims[a.cell_sim[home]];
         if (!kSig && P.stopped) continue;
@@ -788,7 +795,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
         if (flux_only && a.flux_sub >= P.nr_fluxsteps - 1) continue;
         int li, lj, lk;
         cell_loc(P, home, li, lj, lk);
-        if (!kSig && !flux_only && a.has_wall_pots && P.walls_active) {
+        if (!kSig && !flux_only && a.has_wall_pots && P.walls_active && d == 13 && part == 0) {
             for (int i = lane; i < nh; i += 32) {
                 const int g = h0 + i;
                 const float4 p4 = a.pos[g], ax4 = a.aux[g];
@@ -800,7 +807,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                 epot += ew;
             }
         }
-        for (int d = 13; d < 27; d++) {
+        do {   // this warp's task (the continue below leaves it)
             const int ox = d / 9 - 1, oy = (d / 3) % 3 - 1, oz = d % 3 - 1;
             const bool self = d == 13;
             const int mi = (li + ox + P.cdim[0]) % P.cdim[0];
@@ -816,7 +823,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                 sh.z = cell_shift(P, 2, lk, mk);
             }
             const long long total = (long long)nh * nn;
-            for (long long p = lane; p < total; p += 32) {
+            for (long long p = 32 * part + lane; p < total; p += 32 * kOverflowParts) {
                 const int i = (int)(p / nn), j = (int)(p % nn);
                 if (self && i >= j) continue;
                 const int gi = h0 + i, gj = g0 + j;
@@ -900,7 +907,7 @@ __global__ void __launch_bounds__(256) k_pair_overflow(TileArgs T) {
                 atomicAdd(&a.force[gi], fi);
                 atomicAdd(&a.force[gj], fj);
             }
-        }
+        } while (0);
         if (!kSig) flush_red(a.red, P.red_base, epot, vir, lane);
     }
 }

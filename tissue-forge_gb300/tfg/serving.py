@@ -54,7 +54,7 @@ class Request:
     callable that builds it: such a request is built when it arrives, and after submission
     the client keeps only its shape (the server holds the particle data)."""
     __slots__ = ("rid", "t_arrival", "workload", "steps", "t_admit", "t_done", "result", "reductions", "status",
-                 "make")
+                 "make", "t_admit_server")
 
     def __init__(self, rid, t_arrival, workload, steps, make=None):
         self.rid = rid
@@ -63,6 +63,7 @@ class Request:
         self.make = make
         self.steps = int(steps)
         self.t_admit = None
+        self.t_admit_server = None   # admission time on the server's own clock (orders admissions)
         self.t_done = None
         self.result = None
         self.reductions = None
@@ -239,6 +240,7 @@ class Server:
         self.L.tfg_server_request_info(self.h, sid, C.byref(state), C.byref(status), t)
         r.t_done = now
         r.t_admit = max(r.t_arrival, t_submit + (t[1] - t[0])) if t[1] >= 0 else None
+        r.t_admit_server = t[1] if t[1] >= 0 else None
         r.status = int(status.value)
         if state.value == abi.REQ_DONE and self.keep_results:
             n = C.c_int()
