@@ -226,10 +226,10 @@ def fp32_peak(dev):
 
 
 # DRAM traffic of the tiled pair kernel per particle of the arena: one ncu capture of the
-# 256-simulation ensemble pass (2,902,298 particles) read 130.9 MB and wrote 20.8 MB
-# (dram__bytes_read.sum + dram__bytes_write.sum), 52.3 B per particle.  The traffic is the
+# 256-simulation ensemble pass (2,902,298 particles) read 141.3 MB and wrote 26.7 MB
+# (dram__bytes_read.sum + dram__bytes_write.sum), 57.9 B per particle.  The traffic is the
 # particle data read and the forces written, so it scales with the particles, not the pairs.
-PAIR_TRAFFIC_BYTES_PER_PARTICLE = 52.3
+PAIR_TRAFFIC_BYTES_PER_PARTICLE = 57.9
 
 
 def launches_per_step(has_bonds=False, has_angles=False):
@@ -545,7 +545,7 @@ def run_ensemble(args, rank, world, dev, dist):
             "flops_per_pair": FLOPS["table"] + FLOPS["density"], "kernel_ms": phase[1],
             "traffic": PAIR_TRAFFIC_BYTES_PER_PARTICLE * n_tot,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of the tiled "
-                              "kernel on this ensemble (52.3 B per particle), scaled by the particles",
+                              "kernel on this ensemble (57.9 B per particle), scaled by the particles",
             "algorithmic_bytes_per_launch": n_tot * 56,
             "step_hbm": {"achieved_gbs": bytes_alg / (step_ms * 1e-3) / 1e9, "peak_gbs": hbm,
                          "peak_source": hbm_src, "frac": bytes_alg / (step_ms * 1e-3) / 1e9 / hbm,
