@@ -243,48 +243,24 @@ __device__ __forceinline__ void flush_red(double *red, int rb, float &epot, floa
     vir = 0.f;
 }
 
-// Stage particles [g0, g0 + n) of one cell at staged index base on, and return how many were
-// staged.  When pruning, a neighbour particle is staged only when its position in the home
-// frame (x + the task's shift) lies within sqrt(S.box[0].w) of the box S.box that holds
-// every home particle: any other one is farther than the cutoff from every home particle,
-// so no pair is lost.  Staged particles keep their cell order.
+// Stage the home cell's particles [g0, g0 + n) at staged indices 0 .. n-1 (task 13: no shift).
 template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __forceinline__ int stage_body(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task,
-                                          int lane, bool prune) {
-    int kept = 0;
-    const float *sh = S.sh[task];
+__device__ __forceinline__ void stage_home_body(const PairKernelArgs &a, ST &S, int g0, int n, int lane) {
 #pragma unroll 1
-    for (int k0 = 0; k0 < n; k0 += 32) {
-        const int k = k0 + lane;
-        bool keep = k < n;
-        const int g = g0 + (keep ? k : 0);
-        const float4 p = a.pos[g];
-        if (prune) {
-            const float4 lo = S.box[0], hi = S.box[1];
-            const float xs = p.x + sh[0], ys = p.y + sh[1], zs = p.z + sh[2];
-            const float dx = fmaxf(fmaxf(lo.x - xs, xs - hi.x), 0.f);
-            const float dy = fmaxf(fmaxf(lo.y - ys, ys - hi.y), 0.f);
-            const float dz = fmaxf(fmaxf(lo.z - zs, zs - hi.z), 0.f);
-            keep = keep && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) <= lo.w;
+    for (int k = lane; k < n; k += 32) {
+        const int g = g0 + k;
+        const float4 ax = a.aux[g];
+        S.pos[k] = a.pos[g];
+        if (kSig) S.acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        S.gslot[k] = g;
+        S.rad[k] = ax.x;
+        S.seg[k] = 13;
+        if (!kSig && kDPD) {
+            S.vel[k] = a.vel[g];
+            S.id[k] = __float_as_int(ax.w);
         }
-        const uint32_t m = __ballot_sync(0xffffffffu, keep);
-        if (keep) {
-            const int d = base + kept + __popc(m & lanemask_lt());
-            const float4 ax = a.aux[g];
-            S.pos[d] = p;
-            if (kSig) S.acc[d] = make_float4(0.f, 0.f, 0.f, 0.f);
-            S.gslot[d] = g;
-            S.rad[d] = ax.x;
-            S.seg[d] = (uint8_t)task;
-            if (!kSig && kDPD) {
-                S.vel[d] = a.vel[g];
-                S.id[d] = __float_as_int(ax.w);
-            }
-            if (!kSig && kFlux) S.sv[d] = a.sval[g];
-        }
-        kept += __popc(m);
+        if (!kSig && kFlux) S.sv[k] = a.sval[g];
     }
-    return kept;
 }
 
 // Signature variant: add the staged partner counts and id hashes to the per-id totals.
@@ -304,8 +280,11 @@ __device__ __forceinline__ void flush_sig(const PairKernelArgs &a, ST &S, int b0
 
 // Stage entries [f0, f1) of the flat list of this work item's neighbour particles (the
 // forward tasks' offsets and first slots are in S.toff / S.tg0) at staged index base on, in
-// passes of 64 whose loads are in flight together.  Pruning and order are those of
-// stage_body.  Returns the number staged.
+// passes of 64 whose loads are in flight together.  When pruning, a particle is staged only
+// when its position in the home frame (x + its task's shift) lies within sqrt(S.box[0].w) of
+// the box S.box that holds every home particle: any other one is farther than the cutoff
+// from every home particle, so no pair is lost.  Staged particles keep the list order.
+// Returns the number staged.
 template <bool kDPD, bool kFlux, bool kSig, class ST>
 __device__ __forceinline__ int stage_flat_body(const PairKernelArgs &a, ST &S, int base, int f0, int f1, int lane,
                                                bool prune) {
@@ -360,13 +339,12 @@ __device__ __forceinline__ int stage_flat_body(const PairKernelArgs &a, ST &S, i
     return kept;
 }
 
-// Staging runs once per segment, not per pair.  Out of line it keeps the hot candidate and
+// Staging runs once per work item, not per pair.  Out of line it keeps the hot candidate and
 // evaluation loop of the table variants small in instruction cache; the DPD and flux
 // variants, whose evaluation is inlined once, run faster with it inline.
 template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __noinline__ int stage_call(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane,
-                                       bool prune) {
-    return stage_body<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane, prune);
+__device__ __noinline__ void stage_home_call(const PairKernelArgs &a, ST &S, int g0, int n, int lane) {
+    stage_home_body<kDPD, kFlux, kSig>(a, S, g0, n, lane);
 }
 template <bool kDPD, bool kFlux, bool kSig, class ST>
 __device__ __noinline__ int stage_flat_call(const PairKernelArgs &a, ST &S, int base, int f0, int f1, int lane,
@@ -380,10 +358,9 @@ __device__ __forceinline__ int stage_flat(const PairKernelArgs &a, ST &S, int ba
     else return stage_flat_call<kDPD, kFlux, kSig>(a, S, base, f0, f1, lane, prune);
 }
 template <bool kDPD, bool kFlux, bool kSig, class ST>
-__device__ __forceinline__ int stage(const PairKernelArgs &a, ST &S, int base, int g0, int n, int task, int lane,
-                                     bool prune) {
-    if constexpr (kDPD || kFlux) return stage_body<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane, prune);
-    else return stage_call<kDPD, kFlux, kSig>(a, S, base, g0, n, task, lane, prune);
+__device__ __forceinline__ void stage_home(const PairKernelArgs &a, ST &S, int g0, int n, int lane) {
+    if constexpr (kDPD || kFlux) stage_home_body<kDPD, kFlux, kSig>(a, S, g0, n, lane);
+    else stage_home_call<kDPD, kFlux, kSig>(a, S, g0, n, lane);
 }
 
 // kVerlet (table variants): simulations in Verlet mode record, on their rebuild steps, the
@@ -486,7 +463,7 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
             if (kVerlet && lmode == 1 && lane == 0) a.vlen[item] = -1;
             continue;
         }
-        stage<kDPD, kFlux, kSig>(a, S, 0, h0, nh, 13, lane, false);
+        stage_home<kDPD, kFlux, kSig>(a, S, h0, nh, lane);
         __syncwarp();
         // the box that holds every home particle, for the neighbour staging's pruning, with the
         // squared cutoff and a 1e-4 relative margin (far above the few-ulp difference between
