@@ -1093,24 +1093,43 @@ int autotune(tfg_engine *eng, bool splits_only) {
         t.split = TFG_PAIR_HOME_OUTER;
         cand.push_back(t);
     }
+    // one timed launch of a candidate on freshly initialised forces (ms, or < 0 on error)
+    auto trial = [&](const TileTune &tc) -> float {
+        rc = bin(eng, 0);
+        if (rc) return -1.f;
+        PairKernelArgs a = pair_args(eng);
+        cudaEventRecord(eng->ev[0], s);
+        launch_pair_tile(a, tile_plan(eng, tc.split), eng->overflow_list, eng->overflow_count, eng->sms, false, tc, s);
+        cudaEventRecord(eng->ev[1], s);
+        const cudaError_t e = cudaEventSynchronize(eng->ev[1]);
+        if (e != cudaSuccess) {
+            rc = fail(eng, TFG_E_CUDA, std::string("cudaEventSynchronize: ") + cudaGetErrorString(e));
+            return -1.f;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, eng->ev[0], eng->ev[1]);
+        return ms;
+    };
+    // every candidate is timed once; the three fastest are timed twice more and the best of
+    // their three times decides (a third of the launches of timing every candidate three times)
+    std::vector<float> once(cand.size());
+    for (size_t c = 0; c < cand.size(); c++)
+        if ((once[c] = trial(cand[c])) < 0.f) { cudaFree(save); return rc; }
+    std::vector<size_t> order(cand.size());
+    for (size_t c = 0; c < cand.size(); c++) order[c] = c;
+    const size_t top = std::min<size_t>(3, cand.size());
+    std::partial_sort(order.begin(), order.begin() + top, order.end(),
+                      [&](size_t x, size_t y) { return once[x] < once[y]; });
     float best = 1e30f;
-    TileTune best_t;
-    for (const TileTune &tc : cand) {
-        float tmin = 1e30f;
-        for (int rep = 0; rep < 3; rep++) {
-            rc = bin(eng, 0);
-            if (rc) { cudaFree(save); return rc; }
-            PairKernelArgs a = pair_args(eng);
-            cudaEventRecord(eng->ev[0], s);
-            launch_pair_tile(a, tile_plan(eng, tc.split), eng->overflow_list, eng->overflow_count, eng->sms, false,
-                             tc, s);
-            cudaEventRecord(eng->ev[1], s);
-            CK(cudaEventSynchronize(eng->ev[1]));
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, eng->ev[0], eng->ev[1]);
+    TileTune best_t = cand[order[0]];
+    for (size_t k = 0; k < top; k++) {
+        float tmin = once[order[k]];
+        for (int rep = 0; rep < 2; rep++) {
+            const float ms = trial(cand[order[k]]);
+            if (ms < 0.f) { cudaFree(save); return rc; }
             tmin = std::min(tmin, ms);
         }
-        if (tmin < best) { best = tmin; best_t = tc; }
+        if (tmin < best) { best = tmin; best_t = cand[order[k]]; }
     }
     CK(cudaMemcpyAsync(eng->A[eng->cur].sq, save, sizeof(float) * nq, cudaMemcpyDeviceToDevice, s));
     CK(cudaStreamSynchronize(s));
