@@ -15,8 +15,8 @@
 // arithmetic, so the pair set is bit-identical), hits go to a warp-private ring queue, and
 // the queue is evaluated 32 pairs at a time so the force arithmetic runs with full lanes.
 // Each evaluated pair adds the force, number density and flux increments of both partners
-// to the particle arrays with global vector atomics.  Cells above the staging capacity are
-// listed and handled by k_pair_overflow.
+// to the particle arrays with global vector atomics.  Home cells above kHomeCap particles
+// are listed and handled by k_pair_overflow.
 #include <algorithm>
 
 #include "tfg_internal.h"
@@ -92,8 +92,9 @@ struct TileArgs {
     int prune;             // stage only neighbour particles within the cutoff of the home cell's bounding box
 };
 
-// Evaluate one interacting pair, reference orientation I = part_i (home), K = part_j.
-// Returns the I-side and K-side increments (force xyz, density) in fI / fK.
+// Evaluate one candidate pair, reference orientation I = part_i (home), K = part_j.  Returns
+// false when the reference's test puts it beyond the cutoff; otherwise adds the I-side and
+// K-side increments (force xyz, density) to fI / fK and the flux increments to qI / qK.
 template <bool kDPD, bool kFlux, bool kDensity, class ST>
 __device__ __forceinline__ bool eval_pair(const TileArgs &T, const SimParams &P, ST &S, const PotDev *pots,
                                           const float *blob, int I, int K, float &epot, float &vir, float4 &fI,
