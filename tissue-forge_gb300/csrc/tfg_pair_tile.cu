@@ -69,6 +69,9 @@ template <bool kDPD, bool kFlux, bool kSig> struct TileOf {
 static_assert(sizeof(TileOf<false, false, false>::S) * kWarps <= kFourCtaBytes, "table variants: four CTAs per SM");
 static_assert(sizeof(TileOf<true, true, false>::S) * kWarps <= kFourCtaBytes, "DPD and flux variants: four CTAs per SM");
 
+// v in [-1, n] wrapped into [0, n): (v + n) % n for a neighbour offset of at most one cell.
+__device__ __forceinline__ int wrap1(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -410,7 +413,7 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
     if (lane == 0) nxt = atomicAdd(T.overflow_count + 1, grab);
 #pragma unroll 1
     for (int item = base; item < base + grab && item < nitems; item++) {
-        const int home = item / T.split, grp = item - home * T.split;
+        const int home = T.split == 1 ? item : item / T.split, grp = item - home * T.split;
         const int h0 = a.start[home], nh = a.start[home + 1] - h0;
         if (nh == 0) continue;
         const SimParams &P = a.sims[a.cell_sim[home]];
@@ -440,9 +443,10 @@ __global__ void __launch_bounds__(kW * 32, 32 / kW) k_pair_tile(TileArgs T) {
         if (lane < 13) {
             const int d = 14 + lane;
             const int ox = d / 9 - 1, oy = (d / 3) % 3 - 1, oz = d % 3 - 1;
-            const int mi = (li + ox + P.cdim[0]) % P.cdim[0];
-            const int mj = (lj + oy + P.cdim[1]) % P.cdim[1];
-            const int mk = (lk + oz + P.cdim[2]) % P.cdim[2];
+            // periodic wrap of a +-1 offset, without an integer division
+            const int mi = wrap1(li + ox, P.cdim[0]);
+            const int mj = wrap1(lj + oy, P.cdim[1]);
+            const int mk = wrap1(lk + oz, P.cdim[2]);
             const int c = cell_index(P, mi, mj, mk);
             my_g0 = a.start[c];
             my_n = a.start[c + 1] - my_g0;
