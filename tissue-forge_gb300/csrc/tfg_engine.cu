@@ -1110,11 +1110,18 @@ int autotune(tfg_engine *eng, bool splits_only) {
         cudaEventElapsedTime(&ms, eng->ev[0], eng->ev[1]);
         return ms;
     };
-    // every candidate is timed once; the three fastest are timed twice more and the best of
-    // their three times decides (a third of the launches of timing every candidate three times)
+    // every candidate is timed once (three times when a launch takes under 0.5 ms, where one
+    // launch is too noisy to rank and three cost little); the three fastest are then timed
+    // twice more and the best of their times decides
     std::vector<float> once(cand.size());
-    for (size_t c = 0; c < cand.size(); c++)
+    for (size_t c = 0; c < cand.size(); c++) {
         if ((once[c] = trial(cand[c])) < 0.f) { cudaFree(save); return rc; }
+        for (int rep = 0; rep < 2 && once[c] < 0.5f; rep++) {
+            const float ms = trial(cand[c]);
+            if (ms < 0.f) { cudaFree(save); return rc; }
+            once[c] = std::min(once[c], ms);
+        }
+    }
     std::vector<size_t> order(cand.size());
     for (size_t c = 0; c < cand.size(); c++) order[c] = c;
     const size_t top = std::min<size_t>(3, cand.size());
